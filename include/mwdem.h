@@ -1,0 +1,249 @@
+/* mwdem.h -- C ABI of libmwdem.so, the GB300 (sm_103a) implementation of MWDiEM's per-step DEM
+ * hot path: cell-hash broad phase, GJK/EPA narrow phase, spring-dashpot + Coulomb contact force,
+ * quaternion leapfrog integrator.
+ *
+ * Conventions
+ *  - Every pointer argument is a DEVICE pointer unless its comment says "host".
+ *  - Every entry point returns 0 (MWD_OK) or a positive MWD_ERR_* code and never aborts or traps.
+ *    mwd_last_error() returns a one-line description of the last failure on the calling thread.
+ *  - Kernels report data-dependent conditions (EPA did not converge, capacity exceeded, ...) by
+ *    OR-ing MWD_ST_* bits into an optional device status word; the host reads it when it wants.
+ *  - Work is enqueued on the given stream; nothing synchronises unless the comment says so.
+ *  - Array layouts of the "reference layout" entry points are exactly the numpy arrays the
+ *    reference passes to pycuda (row-major, float32 / int32 / float64 as noted).
+ */
+#ifndef MWDEM_H
+#define MWDEM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* mwd_stream_t; /* == cudaStream_t */
+
+enum {
+    MWD_OK = 0,
+    MWD_ERR_INVALID = 1,     /* bad argument (null pointer, size out of range, ...) */
+    MWD_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    MWD_ERR_UNSUPPORTED = 3, /* valid but unsupported (e.g. more hull vertices than the kernel stages) */
+    MWD_ERR_NOMEM = 4        /* device allocation of library scratch failed */
+};
+
+/* device status bits */
+enum {
+    MWD_ST_EPA_NOCONV = 1u,     /* EPA hit the reference's iteration cap (gpu_fine_contact_detection.cu:443-446) */
+    MWD_ST_EPA_OVERFLOW = 2u,   /* EPA needed more polytope faces/vertices than MWD_EPA_FACE_CAP */
+    MWD_ST_GJK_NOCONV = 4u,     /* GJK ran 50 tetrahedron iterations without a decision (.cu:1104) */
+    MWD_ST_PAIR_OVERFLOW = 8u,  /* broad phase produced more candidate pairs than the pair buffer holds */
+    MWD_ST_CELL_RANGE = 16u,    /* a centre's cell key fell outside the scene's dense cell table */
+    MWD_ST_CELL_CROWDED = 32u,  /* a cell held more members than the set-order emulation supports */
+    MWD_ST_BAD_SHAPE = 64u      /* a hull with more vertices than the staging capacity */
+};
+
+#define MWD_EPA_FACE_CAP 128   /* append-only EPA face list per pair */
+#define MWD_EPA_VERT_CAP 32    /* EPA polytope vertices per pair (4 + 25 iterations + 1) */
+#define MWD_HULL_CAP 64        /* hull vertices per side staged in shared memory */
+#define MWD_CELL_CAP 32        /* members per cell handled by the CPython set-order emulation */
+
+/* ------------------------------------------------------------------------------------------
+ * Contact law.  The reference bakes these into its kernel source as literals
+ * (gpu_fine_contact_detection.py:92-103); here they are a POD argument.  mu is both the effective
+ * mass in tc/Gn/Kt/Gt and the Coulomb coefficient, as in the reference (.cu:690-693, .cu:774-788).
+ * ------------------------------------------------------------------------------------------ */
+typedef struct {
+    double Kn, en, et, mu;                     /* particle-particle */
+    double Kn_wall, en_wall, et_wall, mu_wall; /* particle-wall */
+    double dt;                                 /* timestep used in the history update */
+    int32_t n_wall;    /* ids < n_wall are walls (num_particles_wall) */
+    int32_t hist_mode; /* 0: the reference's stride-1 history indexing (.cu:974-976); 1: stride 4 */
+    int32_t lanes;     /* lanes per pair in the narrow phase: 4, 8, 16, 32; 0 = default (8) */
+    int32_t deterministic; /* 1: per-particle sums in pair order instead of float atomics */
+} mwd_contact_params;
+
+/* Per-material constants of the contact law that do not depend on the pair, derived once on the
+ * host from mwd_contact_params with the same float/double operand types the reference uses
+ * (.cu:685-701): tc = sqrt(mu (pi^2 + ln^2 en) / Kn), Gn = -2 mu / tc ln en,
+ * KtA = Kn (pi^2 + ln^2 et) / (pi^2 + ln^2 en).  Per pair the kernel finishes
+ * Kt = KtA / (1/mu + dA^2/IsA + dB^2/IsB) and Gt = -2 / (...) ln et. */
+typedef struct {
+    float Kn_f;   /* (float)Kn */
+    float mu_f;   /* (float)mu */
+    float Gn;     /* normal damping */
+    float ln_et;  /* logf((float)et) */
+    float dt_f;   /* (float)dt */
+    float pad[3];
+    double mu;    /* mu as a double (Coulomb test is done in double, .cu:774) */
+    double inv_mu;
+    double KtA;
+} mwd_material;
+
+/* Fills m[0] (particle-particle) and m[1] (particle-wall) from prm (host pointers). */
+int mwd_derive_material(const mwd_contact_params* prm, mwd_material m[2]);
+
+/* Narrow phase + contact force over per-pair arrays in the reference's layout.
+ *
+ * Replaces gpu_fine_contact_detection.gpu_contact_detection / contact_detection
+ * (LIBRARIES/gpu_fine_contact_detection.py:18-73, LIBRARIES/gpu_fine_contact_detection.cu:874-1322).
+ * Inputs (P = n_pairs, V = num_vertices_max, N = particles):
+ *   A_com, B_com (P,3) f32; A_verts, B_verts (P,V,3) f32 world-frame, zero padded;
+ *   A_vel, B_vel, A_angvel, B_angvel (P,3) f32; A_nv, B_nv, A_id, B_id (P,) i32;
+ *   qA, qB (P,4) f32; IsA, IsB (P,) f32 (moment_of_inertia_size).
+ * In/out: hist (P,4) f32 tangential history; force, torque (N,3) f32, accumulated into.
+ * Out: collision (P,) i32 in {-1, 0, 1}.
+ * Optional (may be NULL): diag (P,10) f32 = depth, normal(3), cpA(3), cpB(3) of colliding pairs;
+ *   status (1,) u32 device status word (OR-ed).
+ * Uses library-owned scratch (allocated on first use per device and kept). */
+int mwd_contact_pairs(int64_t n_pairs, int32_t V, int32_t n_particles,
+                      const float* A_com, const float* B_com, const float* A_verts, const float* B_verts,
+                      const float* A_vel, const float* B_vel, const float* A_angvel, const float* B_angvel,
+                      const int32_t* A_nv, const int32_t* B_nv, const int32_t* A_id, const int32_t* B_id,
+                      float* hist, float* force, float* torque, const float* qA, const float* qB,
+                      const float* IsA, const float* IsB, int32_t* collision,
+                      const mwd_contact_params* prm /* host */, float* diag, uint32_t* status,
+                      mwd_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Integrator over the reference's FP64 arrays.
+ * Replaces gpu_Verlet.gpu_Verlett / Verlet (LIBRARIES/gpu_Verlet.py:18-50, gpu_Verlet.cu:85-431).
+ * ------------------------------------------------------------------------------------------ */
+typedef struct {
+    double dt;
+    double box[6];   /* syssize x_max, x_min, y_max, y_min, z_max, z_min (fly-away box) */
+    int32_t n_min;   /* num_part_min: first integrated row */
+    int32_t n_max;   /* num_part_max: one past the last integrated row */
+    int32_t V;       /* num_vertices_max */
+    int32_t pad;
+} mwd_verlet_params;
+
+/* Arrays (N rows): v, v12, w12bf, wbf, w, F, T, com, dxall (N,3); q12, q, qall (N,4);
+ * verts (N,V,3); mass (N,); Iinv, I (N,3,3); all float64, updated in place like pycuda's InOut.
+ * n_reset (optional, device int32) receives the number of fly-away resets (added to). */
+int mwd_verlet_ref(int32_t N, double* v, double* v12, double* w12bf, double* q12, double* q,
+                   double* qall, double* wbf, double* w, const double* F, const double* T,
+                   double* verts, double* com, const double* mass, const double* Iinv,
+                   const double* I, double* dxall, const mwd_verlet_params* prm /* host */,
+                   int32_t* n_reset, mwd_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Broad phase pieces in the reference's representation.
+ * ------------------------------------------------------------------------------------------ */
+
+/* key[i] = trunc(com_x/csx) + trunc(com_y/csy)*nx + trunc(com_z/csz)*nx*ny for i < N (FP64 divide,
+ * truncation toward zero as numpy's astype(int)).  Replaces MWDiem.py:813-816. */
+int mwd_cell_keys(int32_t N, const double* com, double csx, double csy, double csz, int64_t nx,
+                  int64_t ny, int64_t* keys, mwd_stream_t stream);
+
+/* Wall candidates: for walls k < n_wall and particles j in [n_lo, n_hi), emit [j, k] when
+ * |n_k . (c_j - c_k)| < range, ordered wall-major like MWDiem.py:808-811.
+ * pairs (cap,2) i32; n_out (device int64) receives the total (may exceed cap -> MWD_ST_PAIR_OVERFLOW). */
+int mwd_wall_pairs(int32_t n_wall, int32_t n_lo, int32_t n_hi, const double* com,
+                   const double* wall_normal, const double* wall_center, double range,
+                   int32_t* pairs, int64_t cap, int64_t* n_out, uint32_t* status, mwd_stream_t stream);
+
+/* Cell candidates.  Replaces LIBRARY_Coarse_contact_detection.Linked_cell_hash
+ * (LIBRARIES/LIBRARY_Coarse_contact_detection.py:84-155): ids [n_lo, n_hi) grouped by keys[id];
+ * same-cell pairs oriented in CPython set iteration order, cross-cell pairs for the offsets
+ * +1, +nx, +nx*ny, +nx*ny+1, +nx*ny+1+nx, +nx*ny+nx, +nx+1 with A from the lower-offset cell.
+ * The emitted SET of oriented pairs equals the reference list; the list order is by cell.
+ * keys: (n_hi,) i64 (rows below n_lo ignored).  pairs (cap,2) i32; n_out device int64 (total). */
+int mwd_linked_cell_hash(int32_t n_lo, int32_t n_hi, const int64_t* keys, int64_t nx, int64_t ny,
+                         int32_t* pairs, int64_t cap, int64_t* n_out, uint32_t* status,
+                         mwd_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Device-resident simulation (the GB300-native step).  State lives in HBM as structure-of-arrays
+ * of float4 (FP32) with FP64 centres; shapes are body-frame vertex tables addressed through a CSR
+ * offset per particle; several independent scenes can share one set of arrays ("batched").
+ * A step = broad phase -> narrow phase + force -> integrator, all on one stream, no host sync,
+ * capturable in a CUDA graph.  Replaces the per-step body of MWDiem.py:671-1001.
+ * ------------------------------------------------------------------------------------------ */
+typedef struct {
+    /* per particle row (n rows) */
+    double* pos;         /* (n,4) centre of mass, FP64 */
+    double* dx_all;      /* (n,4) displacement accumulated since the last host sync */
+    float* vel;          /* (n,4) v */
+    float* vel_half;     /* (n,4) v_1/2 */
+    float* w_half_bf;    /* (n,4) omega_1/2, body frame */
+    float* w_bf;         /* (n,4) omega, body frame */
+    float* w;            /* (n,4) omega, world frame */
+    float* q;            /* (n,4) orientation (w,x,y,z) at the full step */
+    float* q_half;       /* (n,4) orientation at the half step */
+    float* q_all;        /* (n,4) rotation accumulated since the last host sync */
+    float* q_acc;        /* (n,4) rotation applied to the body-frame vertices (world = pos + R(q_acc) r0) */
+    float* force;        /* (n,4) contact force accumulator (zeroed by the integrator) */
+    float* torque;       /* (n,4) contact torque accumulator (zeroed by the integrator) */
+    const float* ext_force;  /* (n,4) external force, e.g. mass * g (MWDiem.py:980) */
+    const float* ext_torque; /* (n,4) external torque */
+    const float* inertia;    /* (n,4) body-frame principal moments Ixx, Iyy, Izz, inertia size */
+    const float* inv_inertia;/* (n,4) 1/Ixx, 1/Iyy, 1/Izz, 1/mass */
+    const int32_t* info;     /* (n,) scene id << 1 | is_wall */
+    const double* wall_normal; /* (n,4) plane normal of wall rows (unused for particles) */
+    const int32_t* vert_off; /* (n+1,) CSR offsets into the vertex tables */
+    const float* body_verts; /* (nv,4) body-frame vertices r0 */
+    float* world_verts;      /* (nv,4) world-frame vertices, rewritten by the integrator */
+    int32_t n;
+    int32_t n_verts;
+    int32_t max_verts;       /* largest vertex count of any row (<= MWD_HULL_CAP) */
+    int32_t pad;
+} mwd_state;
+
+typedef struct {
+    double cs[3];        /* cell size x, y, z */
+    double box[6];       /* fly-away box x_max, x_min, y_max, y_min, z_max, z_min */
+    double dt;
+    double wall_range;   /* 6 * max_particlesize (MWDiem.py:810) */
+    int64_t nx, ny;      /* cells per row / per layer (key = xc + yc nx + zc nx ny) */
+    int64_t key_min;     /* smallest key of the dense cell table */
+    int64_t n_keys;      /* dense table length (key_max - key_min + 1) */
+    int64_t cell_base;   /* offset of this scene's table in the global cell arrays */
+    int32_t row_begin, wall_end, row_end, pad; /* rows [row_begin, wall_end) are walls */
+    mwd_contact_params law; /* contact law of the scene */
+    mwd_material mat[2];    /* derived from law by mwd_derive_material (particle, wall) */
+} mwd_scene;
+
+typedef struct {
+    int32_t* cell_count;   /* (total_cells,) zero on entry, left zero on exit */
+    int32_t* cell_start;   /* (total_cells + 1,) */
+    int32_t* cell_of;      /* (n,) global cell of each row, -1 for walls */
+    int32_t* sorted;       /* (n,) rows ordered by cell, members in CPython set order */
+    int32_t* pair_count;   /* (n + 1,) per-row candidate counts, then their exclusive scan */
+    int32_t* pairs;        /* (pair_cap, 2) candidate pairs A, B */
+    int32_t* scan_tmp;     /* scan scratch, mwd_scan_tmp_ints(max(total_cells, n) + 1) ints */
+    int64_t* n_pairs;      /* (1,) candidate count of the last broad phase */
+    uint32_t* status;      /* (1,) status word */
+    int32_t* collision;    /* (pair_cap,) optional contact flags (NULL to skip) */
+    int64_t total_cells;
+    int64_t pair_cap;
+} mwd_work;
+
+/* Scratch ints the device-wide scans need for arrays of n elements. */
+int64_t mwd_scan_tmp_ints(int64_t n);
+
+/* One broad phase over all scenes (rows of every scene; walls excluded from the cell hash). */
+int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes_host,
+                   int32_t n_scenes, mwd_work* work, mwd_stream_t stream);
+
+/* Narrow phase + force over work->pairs[0 .. *work->n_pairs) into st->force/torque. */
+int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work* work,
+                     int32_t lanes, mwd_stream_t stream);
+
+/* Integrator over every non-wall row: consumes force/torque (+ external), updates the state,
+ * rewrites world_verts, zeroes force/torque. */
+int mwd_integrate(mwd_state* st, const mwd_scene* scenes_dev, uint32_t* status, mwd_stream_t stream);
+
+/* broad phase + narrow phase + integrator, n_steps times. */
+int mwd_step(mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes_host, int32_t n_scenes,
+             mwd_work* work, int32_t lanes, int32_t n_steps, mwd_stream_t stream);
+
+/* Library information. */
+const char* mwd_last_error(void);
+int mwd_version(void);
+int32_t mwd_num_sms(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

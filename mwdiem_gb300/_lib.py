@@ -1,0 +1,140 @@
+"""ctypes binding of ``libmwdem.so`` (C ABI in ``include/mwdem.h``).
+
+The library is the only compute path: if it cannot be loaded the import of any GPU entry point
+raises.  Structures below mirror the header field for field.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+from . import build as _build
+
+MWD_OK = 0
+MWD_ERR_INVALID = 1
+MWD_ERR_CUDA = 2
+MWD_ERR_UNSUPPORTED = 3
+MWD_ERR_NOMEM = 4
+
+ST_EPA_NOCONV = 1
+ST_EPA_OVERFLOW = 2
+ST_GJK_NOCONV = 4
+ST_PAIR_OVERFLOW = 8
+ST_CELL_RANGE = 16
+ST_CELL_CROWDED = 32
+ST_BAD_SHAPE = 64
+
+EPA_FACE_CAP = 128
+EPA_VERT_CAP = 32
+HULL_CAP = 64
+CELL_CAP = 32
+
+STATUS_NAMES = {ST_EPA_NOCONV: "EPA_NOCONV", ST_EPA_OVERFLOW: "EPA_OVERFLOW", ST_GJK_NOCONV: "GJK_NOCONV",
+                ST_PAIR_OVERFLOW: "PAIR_OVERFLOW", ST_CELL_RANGE: "CELL_RANGE", ST_CELL_CROWDED: "CELL_CROWDED",
+                ST_BAD_SHAPE: "BAD_SHAPE"}
+
+
+class MwdError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"libmwdem error {code}: {msg}")
+        self.code = code
+
+
+class ContactParams(C.Structure):
+    _fields_ = [("Kn", C.c_double), ("en", C.c_double), ("et", C.c_double), ("mu", C.c_double),
+                ("Kn_wall", C.c_double), ("en_wall", C.c_double), ("et_wall", C.c_double),
+                ("mu_wall", C.c_double), ("dt", C.c_double), ("n_wall", C.c_int32),
+                ("hist_mode", C.c_int32), ("lanes", C.c_int32), ("deterministic", C.c_int32)]
+
+
+class Material(C.Structure):
+    _fields_ = [("Kn_f", C.c_float), ("mu_f", C.c_float), ("Gn", C.c_float), ("ln_et", C.c_float),
+                ("dt_f", C.c_float), ("pad", C.c_float * 3), ("mu", C.c_double), ("inv_mu", C.c_double),
+                ("KtA", C.c_double)]
+
+
+class VerletParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("box", C.c_double * 6), ("n_min", C.c_int32), ("n_max", C.c_int32),
+                ("V", C.c_int32), ("pad", C.c_int32)]
+
+
+_P = C.c_void_p
+
+
+class State(C.Structure):
+    _fields_ = [(n, _P) for n in ("pos", "dx_all", "vel", "vel_half", "w_half_bf", "w_bf", "w", "q", "q_half",
+                                  "q_all", "q_acc", "force", "torque", "ext_force", "ext_torque", "inertia",
+                                  "inv_inertia", "info", "wall_normal", "vert_off", "body_verts", "world_verts")] + \
+               [("n", C.c_int32), ("n_verts", C.c_int32), ("max_verts", C.c_int32), ("pad", C.c_int32)]
+
+
+class Scene(C.Structure):
+    _fields_ = [("cs", C.c_double * 3), ("box", C.c_double * 6), ("dt", C.c_double), ("wall_range", C.c_double),
+                ("nx", C.c_int64), ("ny", C.c_int64), ("key_min", C.c_int64), ("n_keys", C.c_int64),
+                ("cell_base", C.c_int64), ("row_begin", C.c_int32), ("wall_end", C.c_int32),
+                ("row_end", C.c_int32), ("pad", C.c_int32), ("law", ContactParams), ("mat", Material * 2)]
+
+
+class Work(C.Structure):
+    _fields_ = [(n, _P) for n in ("cell_count", "cell_start", "cell_of", "sorted", "pair_count", "pairs",
+                                  "scan_tmp", "n_pairs", "status", "collision")] + \
+               [("total_cells", C.c_int64), ("pair_cap", C.c_int64)]
+
+
+_lock = threading.Lock()
+_handle = None
+
+
+def lib():
+    """Load (building first if needed) ``libmwdem.so``.  Raises if it cannot be built or loaded."""
+    global _handle
+    if _handle is not None:
+        return _handle
+    with _lock:
+        if _handle is not None:
+            return _handle
+        path = _build.build()
+        h = C.CDLL(str(path))
+        i32, i64, d = C.c_int32, C.c_int64, C.c_double
+        sig = {
+            "mwd_last_error": (C.c_char_p, []),
+            "mwd_version": (C.c_int, []),
+            "mwd_num_sms": (i32, []),
+            "mwd_scan_tmp_ints": (i64, [i64]),
+            "mwd_derive_material": (C.c_int, [C.POINTER(ContactParams), C.POINTER(Material)]),
+            "mwd_contact_pairs": (C.c_int, [i64, i32, i32] + [_P] * 20 + [C.POINTER(ContactParams), _P, _P, _P]),
+            "mwd_verlet_ref": (C.c_int, [i32] + [_P] * 16 + [C.POINTER(VerletParams), _P, _P]),
+            "mwd_cell_keys": (C.c_int, [i32, _P, d, d, d, i64, i64, _P, _P]),
+            "mwd_wall_pairs": (C.c_int, [i32, i32, i32, _P, _P, _P, d, _P, i64, _P, _P, _P]),
+            "mwd_linked_cell_hash": (C.c_int, [i32, i32, _P, i64, i64, _P, i64, _P, _P, _P]),
+            "mwd_broadphase": (C.c_int, [C.POINTER(State), _P, _P, i32, C.POINTER(Work), _P]),
+            "mwd_narrow_force": (C.c_int, [C.POINTER(State), _P, C.POINTER(Work), i32, _P]),
+            "mwd_integrate": (C.c_int, [C.POINTER(State), _P, _P, _P]),
+            "mwd_step": (C.c_int, [C.POINTER(State), _P, _P, i32, C.POINTER(Work), i32, i32, _P]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(h, name)
+            f.restype = res
+            f.argtypes = args
+        _handle = h
+        return h
+
+
+EXPORTED = ("mwd_last_error", "mwd_version", "mwd_num_sms", "mwd_scan_tmp_ints", "mwd_derive_material",
+            "mwd_contact_pairs", "mwd_verlet_ref", "mwd_cell_keys", "mwd_wall_pairs", "mwd_linked_cell_hash",
+            "mwd_broadphase", "mwd_narrow_force", "mwd_integrate", "mwd_step")
+
+
+def check(rc: int):
+    if rc != MWD_OK:
+        msg = lib().mwd_last_error()
+        raise MwdError(rc, msg.decode() if msg else "")
+
+
+def lib_path() -> Path:
+    return _build.LIB
+
+
+def status_names(word: int):
+    return [name for bit, name in STATUS_NAMES.items() if word & bit]

@@ -1,0 +1,465 @@
+// Cell-hash broad phase for sm_103a.
+//
+// Reference: MWDiem.py:808-817 (wall candidates, cell keys) and
+// LIBRARIES/LIBRARY_Coarse_contact_detection.py:84-155 (Linked_cell_hash).  The reference groups ids
+// in a dict of Python sets keyed by the integer cell key and walks an 8-cell forward stencil with
+// linear key offsets (+1, +nx, +nx*ny, +nx*ny+1, +nx*ny+1+nx, +nx*ny+nx, +nx+1), no row-wrap
+// guard, same-cell pairs in set iteration order.  Here:
+//
+//   assign   key -> dense cell index (per scene key range), atomic count per cell
+//   scan     exclusive scan of the counts = cell-start table (a one-digit radix/counting sort)
+//   scatter  rows into their cell's slot range (atomicSub brings the counts back to zero)
+//   order    each cell's members sorted by id, then put in CPython 3.12 set iteration order
+//   count    per row: wall candidates + later members of its cell + members of the 7 neighbours
+//   scan     exclusive scan of the counts = output offsets
+//   emit     the same walk, writing [A, B] pairs
+//
+// Every step is deterministic: the pair list depends only on the inputs.
+#include "broad.cuh"
+#include "common.cuh"
+
+namespace mwd {
+
+namespace {
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* sh, int* total)
+{
+    // sh: SCAN_THREADS / 32 ints
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int w = lane < SCAN_THREADS / 32 ? sh[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < SCAN_THREADS / 32) sh[lane] = w;
+    }
+    __syncthreads();
+    int base = wid ? sh[wid - 1] : 0;
+    *total = sh[SCAN_THREADS / 32 - 1];
+    __syncthreads();
+    return base + x - v;
+}
+
+__global__ void scan_reduce_kernel(const int32_t* in, int64_t n, int32_t* block_sums)
+{
+    __shared__ int sh[SCAN_THREADS / 32];
+    int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
+    int s = 0;
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        int64_t i = base + (int64_t)k * SCAN_THREADS + threadIdx.x;
+        if (i < n) s += in[i];
+    }
+    int tot;
+    block_exclusive_scan(s, sh, &tot);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
+}
+
+__global__ void scan_blocks_kernel(int32_t* block_sums, int nb)
+{
+    __shared__ int sh[SCAN_THREADS / 32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nb; base += SCAN_THREADS) {
+        int i = base + threadIdx.x;
+        int v = i < nb ? block_sums[i] : 0;
+        int tot;
+        int ex = block_exclusive_scan(v, sh, &tot);
+        if (i < nb) block_sums[i] = ex + carry;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) block_sums[nb] = carry;
+}
+
+// out[i] = sum(in[0..i)), out[n] = total; in and out may alias
+__global__ void scan_final_kernel(const int32_t* in, int64_t n, const int32_t* block_sums, int32_t* out, int nb,
+                                  int64_t* total_out, int64_t cap, uint32_t* status, uint32_t overflow_bit)
+{
+    __shared__ int sh[SCAN_THREADS / 32];
+    int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    int v[SCAN_ITEMS];
+    int s = 0;
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        int64_t i = base + k;
+        v[k] = i < n ? in[i] : 0;
+        s += v[k];
+    }
+    int tot;
+    int ex = block_exclusive_scan(s, sh, &tot) + block_sums[blockIdx.x];
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        int64_t i = base + k;
+        if (i < n) out[i] = ex;
+        ex += v[k];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        int64_t t = block_sums[nb];
+        out[n] = (int32_t)t;
+        if (total_out) *total_out = t < cap ? t : cap;
+        if (t > cap) set_status(status, overflow_bit);
+    }
+}
+
+// ---------------------------------------------------------------- CPython set iteration order
+
+// Members m[0..k) (ascending ids, the insertion order of the reference's dict walk) reordered as
+// list(set) would list them in CPython 3.12: open addressing on hash(i) = i, up to 9 linear probes
+// when they fit below the mask, then perturbation (perturb >>= 5; i = 5 i + 1 + perturb), table of
+// 8 slots grown to the next power of two above 4*used when fill*5 >= mask*3.
+__device__ void pyset_order(const int* m, int k, int* out)
+{
+    int tab[128];
+    unsigned char used[128];
+    int tmp[128];
+    unsigned char used2[128];
+    unsigned mask = 7;
+    for (int s = 0; s < 128; ++s) used[s] = 0;
+    int fill = 0;
+    for (int e = 0; e < k; ++e) {
+        const uint64_t h = (uint64_t)(uint32_t)m[e];
+        unsigned i = (unsigned)(h & mask);
+        uint64_t perturb = h;
+        for (;;) {
+            unsigned j = i;
+            int probes = (i + 9 <= mask) ? 9 : 0;
+            bool found = false;
+            for (;;) {
+                if (!used[j]) { found = true; break; }
+                if (probes-- == 0) break;
+                j++;
+            }
+            if (found) { i = j; break; }
+            perturb >>= 5;
+            i = (unsigned)((i * 5ull + 1ull + perturb) & mask);
+        }
+        used[i] = 1;
+        tab[i] = m[e];
+        fill++;
+        if ((unsigned)fill * 5u >= mask * 3u) {
+            unsigned newsize = 8, minused = (unsigned)fill * 4u;
+            while (newsize <= minused) newsize <<= 1;
+            unsigned newmask = newsize - 1;
+            for (unsigned s = 0; s < newsize; ++s) used2[s] = 0;
+            for (unsigned s = 0; s <= mask; ++s) {
+                if (!used[s]) continue;
+                const uint64_t hh = (uint64_t)(uint32_t)tab[s];
+                unsigned ii = (unsigned)(hh & newmask);
+                uint64_t pp = hh;
+                for (;;) {
+                    if (!used2[ii]) break;
+                    bool placed = false;
+                    if (ii + 9 <= newmask)
+                        for (unsigned q = 1; q <= 9; ++q)
+                            if (!used2[ii + q]) { ii += q; placed = true; break; }
+                    if (placed) break;
+                    pp >>= 5;
+                    ii = (unsigned)((ii * 5ull + 1ull + pp) & newmask);
+                }
+                used2[ii] = 1;
+                tmp[ii] = tab[s];
+            }
+            mask = newmask;
+            for (unsigned s = 0; s <= mask; ++s) {
+                used[s] = used2[s];
+                tab[s] = tmp[s];
+            }
+        }
+    }
+    int c = 0;
+    for (unsigned s = 0; s <= mask; ++s)
+        if (used[s]) out[c++] = tab[s];
+}
+
+// ---------------------------------------------------------------- broad-phase kernels
+
+__device__ __forceinline__ int scene_of(const BroadArgs& a, int r) { return a.info ? (a.info[r] >> 1) : 0; }
+__device__ __forceinline__ bool is_wall(const BroadArgs& a, int r) { return a.info ? (a.info[r] & 1) : false; }
+
+struct alignas(32) dpos {
+    double x, y, z, w;
+};
+
+__device__ __forceinline__ int64_t row_key(const BroadArgs& a, const mwd_scene& sc, int r)
+{
+    if (a.keys) return a.keys[r];
+    const dpos p = reinterpret_cast<const dpos*>(a.pos)[r];
+    // numpy astype(int): truncation toward zero of the FP64 quotient (MWDiem.py:813-816)
+    const int64_t xc = (int64_t)(p.x / sc.cs[0]);
+    const int64_t yc = (int64_t)(p.y / sc.cs[1]);
+    const int64_t zc = (int64_t)(p.z / sc.cs[2]);
+    return xc + yc * sc.nx + zc * sc.nx * sc.ny;
+}
+
+__global__ void assign_kernel(BroadArgs a)
+{
+    const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.row_hi) return;
+    if (is_wall(a, r)) {
+        a.cell_of[r] = -1;
+        return;
+    }
+    const mwd_scene& sc = a.scenes[scene_of(a, r)];
+    const int64_t local = row_key(a, sc, r) - sc.key_min;
+    if (local < 0 || local >= sc.n_keys) {
+        a.cell_of[r] = -1;
+        set_status(a.status, MWD_ST_CELL_RANGE);
+        return;
+    }
+    const int g = (int)(sc.cell_base + local);
+    a.cell_of[r] = g;
+    atomicAdd(a.cell_count + g, 1);
+}
+
+__global__ void scatter_kernel(BroadArgs a)
+{
+    const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.row_hi) return;
+    const int g = a.cell_of[r];
+    if (g < 0) return;
+    const int slot = atomicSub(a.cell_count + g, 1) - 1;
+    a.scatter_out[a.cell_start[g] + slot] = r;
+}
+
+__global__ void order_kernel(BroadArgs a)
+{
+    const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.row_hi) return;
+    const int g = a.cell_of[r];
+    if (g < 0) return;
+    const int s = a.cell_start[g], e = a.cell_start[g + 1];
+    const int k = e - s;
+    if (k == 1) {
+        a.sorted[s] = r;
+        return;
+    }
+    for (int j = s; j < e; ++j)
+        if (a.scatter_out[j] < r) return;  // the smallest id of the cell orders it
+    if (k > MWD_CELL_CAP) {
+        set_status(a.status, MWD_ST_CELL_CROWDED);
+        // ascending ids (selection by rank; cells this crowded are pathological)
+        for (int j = s; j < e; ++j) {
+            int v = a.scatter_out[j], rank = 0;
+            for (int i = s; i < e; ++i) rank += a.scatter_out[i] < v;
+            a.sorted[s + rank] = v;
+        }
+        return;
+    }
+    int m[MWD_CELL_CAP];
+    for (int j = 0; j < k; ++j) {
+        int v = a.scatter_out[s + j];
+        int i = j;
+        while (i > 0 && m[i - 1] > v) {
+            m[i] = m[i - 1];
+            --i;
+        }
+        m[i] = v;
+    }
+    int o[MWD_CELL_CAP];
+    pyset_order(m, k, o);
+    for (int j = 0; j < k; ++j) a.sorted[s + j] = o[j];
+}
+
+template <bool EMIT>
+__global__ void pairs_kernel(BroadArgs a)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n_sorted = a.cell_start[a.total_cells];
+    if (t >= n_sorted) {
+        if (!EMIT && t < a.row_hi - a.row_lo) a.pair_count[t] = 0;
+        return;
+    }
+    const int r = a.sorted[t];
+    const int g = a.cell_of[r];
+    const mwd_scene& sc = a.scenes[scene_of(a, r)];
+    int c = 0;
+    int64_t out = 0;
+    int32_t* pairs = a.pairs;
+    const int64_t cap = a.pair_cap;
+    if (EMIT) out = a.pair_count[t];
+    auto put = [&](int A, int B) {
+        if (EMIT) {
+            if (out < cap) reinterpret_cast<int2*>(pairs)[out] = make_int2(A, B);
+            ++out;
+        } else {
+            ++c;
+        }
+    };
+    // wall candidates (MWDiem.py:808-811): pair [particle, wall]
+    if (a.walls) {
+        const dpos p = reinterpret_cast<const dpos*>(a.pos)[r];
+        for (int k = sc.row_begin; k < sc.wall_end; ++k) {
+            const dpos wc = reinterpret_cast<const dpos*>(a.pos)[k];
+            const dpos wn = reinterpret_cast<const dpos*>(a.wall_normal)[k];
+            double s = wn.x * (p.x - wc.x) + wn.y * (p.y - wc.y) + wn.z * (p.z - wc.z);
+            if (fabs(s) < sc.wall_range) put(r, k);
+        }
+    }
+    // later members of the same cell, in set order
+    const int cs = a.cell_start[g], ce = a.cell_start[g + 1];
+    for (int j = t + 1; j < ce; ++j) put(r, a.sorted[j]);
+    (void)cs;
+    // forward neighbours
+    const int64_t local = (int64_t)g - sc.cell_base;
+    const int64_t nx = sc.nx, nxy = sc.nx * sc.ny;
+    const int64_t offs[7] = {1, nx, nxy, nxy + 1, nxy + 1 + nx, nxy + nx, nx + 1};
+#pragma unroll
+    for (int o = 0; o < 7; ++o) {
+        const int64_t l2 = local + offs[o];
+        if (l2 < 0 || l2 >= sc.n_keys) continue;
+        const int g2 = (int)(sc.cell_base + l2);
+        const int s2 = a.cell_start[g2], e2 = a.cell_start[g2 + 1];
+        for (int j = s2; j < e2; ++j) put(r, a.sorted[j]);
+    }
+    if (!EMIT) a.pair_count[t] = c;
+}
+
+// wall-major candidates for the reference-layout entry point (MWDiem.py:808-811)
+__global__ void wall_flags_kernel(int n_wall, int n_lo, int n_hi, const double* com, const double* wn, const double* wc,
+                                  double range, int32_t* flags)
+{
+    const int64_t np = n_hi - n_lo;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= np * n_wall) return;
+    const int k = (int)(t / np);
+    const int j = n_lo + (int)(t - (int64_t)k * np);
+    double dx = com[3 * j] - wc[3 * k], dy = com[3 * j + 1] - wc[3 * k + 1], dz = com[3 * j + 2] - wc[3 * k + 2];
+    double s = wn[3 * k] * dx + wn[3 * k + 1] * dy + wn[3 * k + 2] * dz;
+    flags[t] = fabs(s) < range ? 1 : 0;
+}
+
+__global__ void wall_emit_kernel(int n_wall, int n_lo, int n_hi, const int32_t* flags, const int32_t* offs,
+                                 int32_t* pairs, int64_t cap)
+{
+    const int64_t np = n_hi - n_lo;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= np * n_wall) return;
+    if (offs[t + 1] == offs[t]) return;
+    const int k = (int)(t / np);
+    const int j = n_lo + (int)(t - (int64_t)k * np);
+    const int64_t o = offs[t];
+    if (o < cap) reinterpret_cast<int2*>(pairs)[o] = make_int2(j, k);
+}
+
+__global__ void keys_kernel(int N, const double* com, double csx, double csy, double csz, int64_t nx, int64_t ny,
+                            int64_t* keys)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int64_t xc = (int64_t)(com[3 * i] / csx);
+    const int64_t yc = (int64_t)(com[3 * i + 1] / csy);
+    const int64_t zc = (int64_t)(com[3 * i + 2] / csz);
+    keys[i] = xc + yc * nx + zc * nx * ny;
+}
+
+__global__ void minmax_kernel(const int64_t* keys, int lo, int hi, unsigned long long* mm)
+{
+    // mm[0] = min, mm[1] = max of keys in [lo, hi), as order-preserving unsigned values
+    const int i = lo + blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long v_min = ~0ull, v_max = 0ull;
+    if (i < hi) {
+        unsigned long long u = (unsigned long long)keys[i] ^ 0x8000000000000000ull;
+        v_min = v_max = u;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long a = __shfl_xor_sync(0xffffffffu, v_min, o);
+        unsigned long long b = __shfl_xor_sync(0xffffffffu, v_max, o);
+        v_min = a < v_min ? a : v_min;
+        v_max = b > v_max ? b : v_max;
+    }
+    if ((threadIdx.x & 31) == 0 && i - (int)(threadIdx.x & 31) < hi) {
+        atomicMin(mm, v_min);
+        atomicMax(mm + 1, v_max);
+    }
+}
+
+inline unsigned blocks(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+int64_t scan_tmp_ints(int64_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 2; }
+
+int launch_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* tmp, int64_t* total_out, int64_t cap,
+                uint32_t* status, uint32_t overflow_bit, cudaStream_t s)
+{
+    const int nb = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
+    const int nbl = nb > 0 ? nb : 1;
+    scan_reduce_kernel<<<nbl, SCAN_THREADS, 0, s>>>(in, n, tmp);
+    scan_blocks_kernel<<<1, SCAN_THREADS, 0, s>>>(tmp, nbl);
+    scan_final_kernel<<<nbl, SCAN_THREADS, 0, s>>>(in, n, tmp, out, nbl, total_out, cap, status, overflow_bit);
+    MWD_CUDA(cudaGetLastError());
+    return MWD_OK;
+}
+
+int launch_broad(const BroadArgs& a, cudaStream_t s)
+{
+    const int T = 256;
+    const int64_t rows = a.row_hi - a.row_lo;
+    if (rows <= 0 || a.total_cells <= 0) {
+        MWD_CUDA(cudaMemsetAsync(a.n_pairs, 0, sizeof(int64_t), s));
+        return MWD_OK;
+    }
+    assign_kernel<<<blocks(rows, T), T, 0, s>>>(a);
+    int rc = launch_scan(a.cell_count, a.total_cells, a.cell_start, a.scan_tmp, nullptr, INT64_MAX, nullptr, 0, s);
+    if (rc) return rc;
+    scatter_kernel<<<blocks(rows, T), T, 0, s>>>(a);
+    order_kernel<<<blocks(rows, T), T, 0, s>>>(a);
+    // rows that have a cell are at most `rows`; threads past cell_start[total] exit
+    pairs_kernel<false><<<blocks(rows, T), T, 0, s>>>(a);
+    rc = launch_scan(a.pair_count, rows, a.pair_count, a.scan_tmp, a.n_pairs, a.pair_cap, a.status,
+                     MWD_ST_PAIR_OVERFLOW, s);
+    if (rc) return rc;
+    pairs_kernel<true><<<blocks(rows, T), T, 0, s>>>(a);
+    MWD_CUDA(cudaGetLastError());
+    return MWD_OK;
+}
+
+int launch_keys(int N, const double* com, double csx, double csy, double csz, int64_t nx, int64_t ny, int64_t* keys,
+                cudaStream_t s)
+{
+    if (N <= 0) return MWD_OK;
+    keys_kernel<<<blocks(N, 256), 256, 0, s>>>(N, com, csx, csy, csz, nx, ny, keys);
+    MWD_CUDA(cudaGetLastError());
+    return MWD_OK;
+}
+
+int launch_minmax(const int64_t* keys, int lo, int hi, unsigned long long* mm, cudaStream_t s)
+{
+    if (hi <= lo) return MWD_OK;
+    minmax_kernel<<<blocks(hi - lo, 256), 256, 0, s>>>(keys, lo, hi, mm);
+    MWD_CUDA(cudaGetLastError());
+    return MWD_OK;
+}
+
+int launch_wall_pairs(int n_wall, int n_lo, int n_hi, const double* com, const double* wn, const double* wc,
+                      double range, int32_t* flags, int32_t* offs, int32_t* tmp, int32_t* pairs, int64_t cap,
+                      int64_t* n_out, uint32_t* status, cudaStream_t s)
+{
+    const int64_t total = (int64_t)n_wall * (n_hi - n_lo);
+    if (total <= 0) {
+        MWD_CUDA(cudaMemsetAsync(n_out, 0, sizeof(int64_t), s));
+        return MWD_OK;
+    }
+    wall_flags_kernel<<<blocks(total, 256), 256, 0, s>>>(n_wall, n_lo, n_hi, com, wn, wc, range, flags);
+    int rc = launch_scan(flags, total, offs, tmp, n_out, cap, status, MWD_ST_PAIR_OVERFLOW, s);
+    if (rc) return rc;
+    wall_emit_kernel<<<blocks(total, 256), 256, 0, s>>>(n_wall, n_lo, n_hi, flags, offs, pairs, cap);
+    MWD_CUDA(cudaGetLastError());
+    return MWD_OK;
+}
+
+}  // namespace mwd

@@ -1,0 +1,42 @@
+// Launch arguments of the broad-phase kernels (internal to libmwdem).
+#pragma once
+
+#include "common.cuh"
+
+namespace mwd {
+
+struct BroadArgs {
+    int32_t row_lo, row_hi;      // rows considered
+    const int64_t* keys;         // given keys per row (reference-layout entry) or NULL: computed from pos
+    const double* pos;           // (n,4) centres (FP64), used when keys == NULL and for walls
+    const double* wall_normal;   // (n,4) wall normals
+    const int32_t* info;         // (n,) scene << 1 | is_wall, or NULL: one scene, no walls
+    const mwd_scene* scenes;     // device scene table
+    int32_t walls;               // 1: emit wall candidates
+    int32_t pad;
+    int32_t* cell_count;         // (total_cells,) zero on entry and on exit
+    int32_t* cell_start;         // (total_cells+1,)
+    int32_t* cell_of;            // (n,)
+    int32_t* scatter_out;        // (n,) rows scattered into their cells (any order within a cell)
+    int32_t* sorted;             // (n,) rows in cell order, members in set order
+    int32_t* pair_count;         // (rows+1,)
+    int32_t* scan_tmp;
+    int32_t* pairs;              // (pair_cap,2)
+    int64_t* n_pairs;
+    uint32_t* status;
+    int64_t total_cells;
+    int64_t pair_cap;
+};
+
+int64_t scan_tmp_ints(int64_t n);
+int launch_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* tmp, int64_t* total_out, int64_t cap,
+                uint32_t* status, uint32_t overflow_bit, cudaStream_t s);
+int launch_broad(const BroadArgs& a, cudaStream_t s);
+int launch_keys(int N, const double* com, double csx, double csy, double csz, int64_t nx, int64_t ny, int64_t* keys,
+                cudaStream_t s);
+int launch_minmax(const int64_t* keys, int lo, int hi, unsigned long long* mm, cudaStream_t s);
+int launch_wall_pairs(int n_wall, int n_lo, int n_hi, const double* com, const double* wn, const double* wc,
+                      double range, int32_t* flags, int32_t* offs, int32_t* tmp, int32_t* pairs, int64_t cap,
+                      int64_t* n_out, uint32_t* status, cudaStream_t s);
+
+}  // namespace mwd

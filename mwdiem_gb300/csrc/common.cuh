@@ -1,0 +1,77 @@
+// Shared device helpers for libmwdem (sm_103a).
+//
+// Every translation unit of the library is compiled with --fmad=false and IEEE division/sqrt
+// (no -use_fast_math): the narrow phase must round exactly like the reference kernel's
+// operation sequence, which the oracle evaluates on the CPU without FMA contraction.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/mwdem.h"
+
+namespace mwd {
+
+struct f3 {
+    float x, y, z;
+};
+
+__host__ __device__ __forceinline__ f3 mk3(float x, float y, float z)
+{
+    f3 r;
+    r.x = x;
+    r.y = y;
+    r.z = z;
+    return r;
+}
+__host__ __device__ __forceinline__ f3 operator+(f3 a, f3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ f3 operator-(f3 a, f3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ f3 operator*(f3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+__host__ __device__ __forceinline__ f3 operator/(f3 a, float s) { return mk3(a.x / s, a.y / s, a.z / s); }
+// left-to-right sum of products, the reference's dot (gpu_fine_contact_detection.cu:21-24)
+__host__ __device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ __forceinline__ f3 cross(f3 a, f3 b)
+{
+    return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__host__ __device__ __forceinline__ float norm2(f3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+__device__ __forceinline__ f3 xyz(float4 v) { return mk3(v.x, v.y, v.z); }
+__device__ __forceinline__ float4 f4(f3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
+
+// Hamilton product (w, x, y, z), operand order of gpu_fine_contact_detection.cu:613-624:
+// vector part = b*a0 + a*b0 + a x b, scalar part = a0 b0 - a.b
+__host__ __device__ __forceinline__ float4 qmul(float4 a, float4 b)
+{
+    f3 u = mk3(a.y, a.z, a.w), v = mk3(b.y, b.z, b.w);
+    f3 s = (v * a.x + u * b.x) + cross(u, v);
+    float f = a.x * b.x - dot(u, v);
+    return make_float4(f, s.x, s.y, s.z);
+}
+__host__ __device__ __forceinline__ float4 qconj(float4 q) { return make_float4(q.x, q.y * (-1.f), q.z * (-1.f), q.w * (-1.f)); }
+// q1 (0,v) q2, vector part (gpu_fine_contact_detection.cu:626-643)
+__host__ __device__ __forceinline__ f3 qtrip(float4 q1, f3 v, float4 q2)
+{
+    float4 m1 = qmul(make_float4(0.f, v.x, v.y, v.z), q2);
+    float4 m2 = qmul(q1, m1);
+    return mk3(m2.y, m2.z, m2.w);
+}
+
+__device__ __forceinline__ void set_status(uint32_t* st, uint32_t bits)
+{
+    if (st && bits) atomicOr(st, bits);
+}
+
+}  // namespace mwd
+
+// error plumbing shared by the host side of every translation unit
+namespace mwd {
+void set_error(const char* fmt, ...);
+int cuda_check(cudaError_t e, const char* what);
+int num_sms();
+}  // namespace mwd
+
+#define MWD_CUDA(call)                                                  \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) return ::mwd::cuda_check(e_, #call);     \
+    } while (0)

@@ -1,0 +1,356 @@
+// Quaternion leapfrog integrator (gpu_Verlet.cu:85-431), two variants:
+//
+//  * verlet_ref_kernel -- FP64 over the reference's own arrays (the drop-in for gpu_Verlet.Verlet_GPU).
+//    Same operation sequence as the reference; the per-vertex rotation of the world-frame vertex
+//    table (gpu_Verlet.cu:279-323) is done block-cooperatively so the (N,V,3) array is read and
+//    written with coalesced accesses instead of one thread walking V vertices.
+//
+//  * integrate_kernel -- FP32 state in float4 structure-of-arrays with FP64 centres (the
+//    device-resident step).  Instead of rotating every world vertex by q each step (which compounds
+//    the rotation, gpu_Verlet.cu:279-305), it keeps q_acc = q_k (x) q_acc, the product of those
+//    rotations, and regenerates world = pos + R(q_acc) r0 from the body-frame table: the same
+//    vertices, without accumulating rounding in the vertex coordinates.  Walls are not integrated
+//    (rows below num_part_min, gpu_Verlet.cu:110).  The force/torque accumulators are consumed and
+//    zeroed for the next step.
+#include "common.cuh"
+#include "integrate.cuh"
+
+namespace mwd {
+
+namespace {
+
+struct d3 {
+    double x, y, z;
+};
+__device__ __forceinline__ d3 dm(double x, double y, double z)
+{
+    d3 r;
+    r.x = x;
+    r.y = y;
+    r.z = z;
+    return r;
+}
+__device__ __forceinline__ d3 operator+(d3 a, d3 b) { return dm(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ d3 operator-(d3 a, d3 b) { return dm(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ d3 operator*(d3 a, double s) { return dm(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ d3 operator/(d3 a, double s) { return dm(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ double ddot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ d3 dcross(d3 a, d3 b) { return dm(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+__device__ __forceinline__ d3 dld(const double* p) { return dm(p[0], p[1], p[2]); }
+__device__ __forceinline__ void dst(double* p, d3 v) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
+
+struct dq {
+    double w, x, y, z;
+};
+// Hamilton product, operand order of gpu_Verlet.cu:43-54
+__device__ __forceinline__ dq dqmul(dq a, dq b)
+{
+    d3 u = dm(a.x, a.y, a.z), v = dm(b.x, b.y, b.z);
+    d3 s = (v * a.w + u * b.w) + dcross(u, v);
+    dq r;
+    r.w = a.w * b.w - ddot(u, v);
+    r.x = s.x;
+    r.y = s.y;
+    r.z = s.z;
+    return r;
+}
+__device__ __forceinline__ dq dqinv(dq q)
+{
+    dq r;
+    r.w = q.w;
+    r.x = q.x * (-1);
+    r.y = q.y * (-1);
+    r.z = q.z * (-1);
+    return r;
+}
+__device__ __forceinline__ d3 dqtrip(dq q1, d3 v, dq q2)
+{
+    dq vq;
+    vq.w = 0;
+    vq.x = v.x;
+    vq.y = v.y;
+    vq.z = v.z;
+    dq m = dqmul(q1, dqmul(vq, q2));
+    return dm(m.x, m.y, m.z);
+}
+__device__ __forceinline__ dq dqld(const double* p)
+{
+    dq q;
+    q.w = p[0];
+    q.x = p[1];
+    q.y = p[2];
+    q.z = p[3];
+    return q;
+}
+__device__ __forceinline__ void dqst(double* p, dq q)
+{
+    p[0] = q.w;
+    p[1] = q.x;
+    p[2] = q.y;
+    p[3] = q.z;
+}
+__device__ __forceinline__ d3 matvec(const double* M, d3 v)
+{
+    return dm(M[0] * v.x + M[1] * v.y + M[2] * v.z, M[3] * v.x + M[4] * v.y + M[5] * v.z, M[6] * v.x + M[7] * v.y + M[8] * v.z);
+}
+
+constexpr int RB = 128;  // rows per block
+
+__global__ void __launch_bounds__(RB) verlet_ref_kernel(VerletRefArgs a)
+{
+    __shared__ dq s_q[RB];
+    __shared__ d3 s_c[RB];
+    __shared__ d3 s_dx[RB];
+    __shared__ int s_mode[RB];  // 0 inactive, 1 active, 2 active + fly-away reset
+    const int P = blockIdx.x * RB + threadIdx.x;
+    const double dt = a.p.dt;
+    int mode = 0;
+    if (P < a.N && P >= a.p.n_min && P < a.p.n_max) {
+        d3 vel12 = dld(a.v12 + 3 * P), om12bf = dld(a.w12bf + 3 * P), ombf = dld(a.wbf + 3 * P);
+        d3 om = dld(a.w + 3 * P), c = dld(a.com + 3 * P);
+        d3 f = dld(a.F + 3 * P), t = dld(a.T + 3 * P);
+        const double m = a.mass[P];
+        const double* Mi = a.Iinv + 9 * P;
+        const double* Mm = a.I + 9 * P;
+        dq qq = dqld(a.q + 4 * P), qh = dqld(a.q12 + 4 * P);
+        d3 dxa = dld(a.dxall + 3 * P);
+
+        d3 v32 = vel12 + ((f * 1) / m) * dt;
+        dq qi = dqinv(qq);
+        d3 tbf = dqtrip(qi, t, qq);
+        d3 p1 = matvec(Mm, ombf);
+        d3 p2 = tbf - dcross(ombf, p1);
+        d3 alpha = matvec(Mi, p2);
+        d3 om32bf = om12bf + alpha * dt;
+        double wn = sqrt(om.x * om.x + om.y * om.y + om.z * om.z);
+        d3 h = dm(0, 0, 0);
+        if (wn != 0) h = (om / wn) * sin(wn * dt / 2);
+        dq rq;
+        rq.w = cos(wn * dt / 2);
+        rq.x = h.x;
+        rq.y = h.y;
+        rq.z = h.z;
+        dq q32 = dqmul(rq, qh);
+        vel12 = v32;
+        qh = q32;
+        om12bf = om32bf;
+        d3 dx = vel12 * dt;
+        dxa = dxa + dx;
+        d3 om34bf = om12bf + ((alpha * dt) * 1) / 4;
+        d3 om34 = dqtrip(qh, om34bf, dqinv(qh));
+        double wn34 = sqrt(om34.x * om34.x + om34.y * om34.y + om34.z * om34.z);
+        d3 h2 = dm(0, 0, 0);
+        if (wn34 != 0) h2 = (om34 / wn34) * sin(wn34 * dt / 4);
+        dq rq2;
+        rq2.w = cos(wn34 * dt / 4);
+        rq2.x = h2.x;
+        rq2.y = h2.y;
+        rq2.z = h2.z;
+        dq qold = qq;
+        qq = dqmul(rq2, qh);
+        dq qa = dqmul(qq, qold);
+        ombf = om12bf + ((alpha * dt) * 1) / 2;
+        om = dqtrip(qq, ombf, dqinv(qq));
+        d3 vel = vel12 + (f * dt) / m;
+        const d3 c_old = c;
+        c = c + dx;
+        mode = 1;
+        const double* box = a.p.box;
+        if (c.x > box[0] || c.x < box[1] || c.y > box[2] || c.y < box[3] || c.z > box[4] || c.z < box[5]) {
+            mode = 2;
+            vel = dm(0, 0, 0);
+            vel12 = vel;
+            om12bf = vel;
+            ombf = vel;
+            om = vel;
+            c = c + dx * (-1);
+            if (a.n_reset) atomicAdd(a.n_reset, 1);
+        }
+        dst(a.v + 3 * P, vel);
+        dst(a.v12 + 3 * P, vel12);
+        dst(a.w12bf + 3 * P, om12bf);
+        dst(a.com + 3 * P, c);
+        dst(a.dxall + 3 * P, dxa);
+        dst(a.wbf + 3 * P, ombf);
+        dst(a.w + 3 * P, om);
+        dqst(a.q12 + 4 * P, qh);
+        dqst(a.q + 4 * P, qq);
+        dqst(a.qall + 4 * P, qa);
+        s_q[threadIdx.x] = qq;
+        s_c[threadIdx.x] = c_old;
+        s_dx[threadIdx.x] = dx;
+    }
+    s_mode[threadIdx.x] = mode;
+    __syncthreads();
+    // vertices of this block's rows: rotate about the old centre, then translate (gpu_Verlet.cu:279-352)
+    const int V = a.p.V;
+    const int p0 = blockIdx.x * RB;
+    const int rows = min(RB, a.N - p0);
+    for (int j = threadIdx.x; j < rows * V; j += RB) {
+        const int r = j / V;
+        const int md = s_mode[r];
+        if (!md) continue;
+        double* vp = a.verts + ((size_t)(p0 + r) * V + (j - r * V)) * 3;
+        const dq q = s_q[r];
+        const d3 c = s_c[r], dx = s_dx[r];
+        d3 v = dqtrip(q, dld(vp) - c, dqinv(q)) + c;
+        v = v + dx;
+        if (md == 2) v = v + dx * (-1);
+        dst(vp, v);
+    }
+}
+
+// ------------------------------------------------------------------ FP32 device-resident step
+
+__device__ __forceinline__ float4 ld4(const float* p, int i) { return reinterpret_cast<const float4*>(p)[i]; }
+__device__ __forceinline__ void st4(float* p, int i, float4 v) { reinterpret_cast<float4*>(p)[i] = v; }
+
+struct alignas(32) dpos {
+    double x, y, z, w;
+};
+
+// rotation increment [cos(|w| s), sin(|w| s) w/|w|]
+__device__ __forceinline__ float4 rot_increment(f3 w, float s)
+{
+    float wn = sqrtf(w.x * w.x + w.y * w.y + w.z * w.z);
+    float sn, cs;
+    sincosf(wn * s, &sn, &cs);
+    f3 h = mk3(0.f, 0.f, 0.f);
+    if (wn != 0.f) h = (w / wn) * sn;
+    return make_float4(cs, h.x, h.y, h.z);
+}
+
+__global__ void __launch_bounds__(RB) integrate_kernel(mwd_state st, const mwd_scene* __restrict__ scenes,
+                                                       uint32_t* status)
+{
+    __shared__ float s_R[RB][9];
+    __shared__ float s_c[RB][6];  // centre split hi/lo per axis
+    __shared__ int s_off[RB + 1];
+    const int P = blockIdx.x * RB + threadIdx.x;
+    const int p0 = blockIdx.x * RB;
+    const int rows = min(RB, st.n - p0);
+    if (P < st.n) {
+        const int info = st.info[P];
+        dpos pos = reinterpret_cast<const dpos*>(st.pos)[P];
+        float4 qacc = ld4(st.q_acc, P);
+        if (!(info & 1)) {
+            const mwd_scene& sc = scenes[info >> 1];
+            const float dt = (float)sc.dt;
+            float4 Fa = ld4(st.force, P), Ta = ld4(st.torque, P);
+            float4 Fe = ld4(st.ext_force, P), Te = ld4(st.ext_torque, P);
+            f3 F = mk3(Fa.x + Fe.x, Fa.y + Fe.y, Fa.z + Fe.z);
+            f3 T = mk3(Ta.x + Te.x, Ta.y + Te.y, Ta.z + Te.z);
+            float4 I = ld4(st.inertia, P), Ii = ld4(st.inv_inertia, P);
+            const float invm = Ii.w;
+            f3 vh = xyz(ld4(st.vel_half, P));
+            f3 whbf = xyz(ld4(st.w_half_bf, P));
+            f3 wbf = xyz(ld4(st.w_bf, P));
+            f3 w = xyz(ld4(st.w, P));
+            float4 q = ld4(st.q, P), qh = ld4(st.q_half, P), qall = ld4(st.q_all, P);
+            dpos dxall = reinterpret_cast<const dpos*>(st.dx_all)[P];
+
+            f3 v32 = vh + F * (invm * dt);
+            f3 tbf = qtrip(qconj(q), T, q);
+            f3 p1 = mk3(I.x * wbf.x, I.y * wbf.y, I.z * wbf.z);
+            f3 p2 = tbf - cross(wbf, p1);
+            f3 alpha = mk3(Ii.x * p2.x, Ii.y * p2.y, Ii.z * p2.z);
+            f3 w32bf = whbf + alpha * dt;
+            float4 q32 = qmul(rot_increment(w, dt * 0.5f), qh);
+            vh = v32;
+            qh = q32;
+            whbf = w32bf;
+            f3 dx = vh * dt;
+            dxall.x += (double)dx.x;
+            dxall.y += (double)dx.y;
+            dxall.z += (double)dx.z;
+            f3 w34bf = whbf + alpha * (dt * 0.25f);
+            f3 w34 = qtrip(qh, w34bf, qconj(qh));
+            float4 qold = q;
+            q = qmul(rot_increment(w34, dt * 0.25f), qh);
+            qall = qmul(q, qold);
+            wbf = whbf + alpha * (dt * 0.5f);
+            w = qtrip(q, wbf, qconj(q));
+            f3 v = vh + F * (invm * dt);
+            // vertices compound the rotation q every step (gpu_Verlet.cu:279-305): q_acc <- q q_acc
+            qacc = qmul(q, qacc);
+            float qn = rsqrtf(qacc.x * qacc.x + qacc.y * qacc.y + qacc.z * qacc.z + qacc.w * qacc.w);
+            qacc = make_float4(qacc.x * qn, qacc.y * qn, qacc.z * qn, qacc.w * qn);
+            dpos np;
+            np.x = pos.x + (double)dx.x;
+            np.y = pos.y + (double)dx.y;
+            np.z = pos.z + (double)dx.z;
+            np.w = pos.w;
+            if (np.x > sc.box[0] || np.x < sc.box[1] || np.y > sc.box[2] || np.y < sc.box[3] || np.z > sc.box[4] ||
+                np.z < sc.box[5]) {
+                // fly-away reset (gpu_Verlet.cu:338-352): stop the particle, undo the move
+                v = vh = whbf = wbf = w = mk3(0.f, 0.f, 0.f);
+                np = pos;
+            }
+            pos = np;
+            reinterpret_cast<dpos*>(st.pos)[P] = pos;
+            reinterpret_cast<dpos*>(st.dx_all)[P] = dxall;
+            st4(st.vel, P, f4(v, 0.f));
+            st4(st.vel_half, P, f4(vh, 0.f));
+            st4(st.w_half_bf, P, f4(whbf, 0.f));
+            st4(st.w_bf, P, f4(wbf, 0.f));
+            st4(st.w, P, f4(w, 0.f));
+            st4(st.q, P, q);
+            st4(st.q_half, P, qh);
+            st4(st.q_all, P, qall);
+            st4(st.q_acc, P, qacc);
+            st4(st.force, P, make_float4(0.f, 0.f, 0.f, 0.f));
+            st4(st.torque, P, make_float4(0.f, 0.f, 0.f, 0.f));
+        }
+        // rotation matrix of q_acc and the centre as hi + lo floats, for the vertex pass
+        const float qw = qacc.x, qx = qacc.y, qy = qacc.z, qz = qacc.w;
+        float* R = s_R[threadIdx.x];
+        R[0] = 1.f - 2.f * (qy * qy + qz * qz); R[1] = 2.f * (qx * qy - qw * qz); R[2] = 2.f * (qx * qz + qw * qy);
+        R[3] = 2.f * (qx * qy + qw * qz); R[4] = 1.f - 2.f * (qx * qx + qz * qz); R[5] = 2.f * (qy * qz - qw * qx);
+        R[6] = 2.f * (qx * qz - qw * qy); R[7] = 2.f * (qy * qz + qw * qx); R[8] = 1.f - 2.f * (qx * qx + qy * qy);
+        float hx = (float)pos.x, hy = (float)pos.y, hz = (float)pos.z;
+        s_c[threadIdx.x][0] = hx; s_c[threadIdx.x][1] = (float)(pos.x - (double)hx);
+        s_c[threadIdx.x][2] = hy; s_c[threadIdx.x][3] = (float)(pos.y - (double)hy);
+        s_c[threadIdx.x][4] = hz; s_c[threadIdx.x][5] = (float)(pos.z - (double)hz);
+        s_off[threadIdx.x] = st.vert_off[P];
+    }
+    if (threadIdx.x == 0) s_off[rows] = st.vert_off[p0 + rows];
+    __syncthreads();
+    const int v0 = s_off[0], v1 = s_off[rows];
+    const float4* bv = reinterpret_cast<const float4*>(st.body_verts);
+    float4* wv = reinterpret_cast<float4*>(st.world_verts);
+    for (int j = v0 + threadIdx.x; j < v1; j += RB) {
+        // owner row: last r with s_off[r] <= j
+        int lo = 0, hi = rows - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (s_off[mid] <= j) lo = mid; else hi = mid - 1;
+        }
+        const float* R = s_R[lo];
+        const float* c = s_c[lo];
+        float4 r0 = bv[j];
+        float rx = R[0] * r0.x + R[1] * r0.y + R[2] * r0.z;
+        float ry = R[3] * r0.x + R[4] * r0.y + R[5] * r0.z;
+        float rz = R[6] * r0.x + R[7] * r0.y + R[8] * r0.z;
+        wv[j] = make_float4(c[0] + (rx + c[1]), c[2] + (ry + c[3]), c[4] + (rz + c[5]), 0.f);
+    }
+}
+
+}  // namespace
+
+int launch_verlet_ref(const VerletRefArgs& a, cudaStream_t s)
+{
+    if (a.N <= 0) return MWD_OK;
+    verlet_ref_kernel<<<(a.N + RB - 1) / RB, RB, 0, s>>>(a);
+    MWD_CUDA(cudaGetLastError());
+    return MWD_OK;
+}
+
+int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, cudaStream_t s)
+{
+    if (st.n <= 0) return MWD_OK;
+    integrate_kernel<<<(st.n + RB - 1) / RB, RB, 0, s>>>(st, scenes, status);
+    MWD_CUDA(cudaGetLastError());
+    return MWD_OK;
+}
+
+}  // namespace mwd

@@ -1,0 +1,22 @@
+// Launch arguments of the integrator kernels (internal to libmwdem).
+#pragma once
+
+#include "common.cuh"
+
+namespace mwd {
+
+struct VerletRefArgs {
+    int32_t N;
+    double *v, *v12, *w12bf, *q12, *q, *qall, *wbf, *w;
+    const double *F, *T;
+    double *verts, *com;
+    const double *mass, *Iinv, *I;
+    double* dxall;
+    int32_t* n_reset;
+    mwd_verlet_params p;
+};
+
+int launch_verlet_ref(const VerletRefArgs& a, cudaStream_t s);
+int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, cudaStream_t s);
+
+}  // namespace mwd

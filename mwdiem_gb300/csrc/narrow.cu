@@ -1,0 +1,725 @@
+// Narrow phase (GJK + EPA) and contact force, warp-cooperative, for sm_103a.
+//
+// Algorithm: LIBRARIES/gpu_fine_contact_detection.cu (GJK driver :996-1288, simplex tests :103-268,
+// EPA :270-603, force :647-871).  The decisions and the floating-point operation sequence are the
+// reference's, so contact flags, depths, normals and forces round exactly as the reference kernel
+// evaluated without FMA contraction.  The execution model is not:
+//
+//  * a group of LPP lanes (4/8/16/32) works on one pair; a block holds 128/LPP groups and the grid
+//    strides over the pair list;
+//  * both hulls are staged once per pair in shared memory as float4; every support query is a
+//    strided scan by the group's lanes plus a butterfly argmax on (value desc, index asc), which
+//    reproduces the reference's strict-'>' first-index tie break;
+//  * the simplex logic runs redundantly (identically) on every lane of the group, so control flow
+//    stays group-uniform;
+//  * EPA keeps an append-only face list of MWD_EPA_FACE_CAP faces in shared memory (the reference's
+//    T[50]/n[50]/dist[50] overflow past 50 faces); the face scan, the visibility test, the horizon
+//    edge count (the reference's 50x50 delpair matrix, replaced by counting over the deleted-face
+//    list) and the new faces are computed lane-parallel, with ballots to keep the reference's face
+//    order;
+//  * force/torque are accumulated with float atomics (skipped for wall rows in table mode, whose
+//    forces the reference discards, MWDiem.py:977-978).
+#include <float.h>
+
+#include "common.cuh"
+#include "narrow.cuh"
+
+namespace mwd {
+
+namespace {
+
+constexpr int FCAP = MWD_EPA_FACE_CAP;
+constexpr int VCAP = MWD_EPA_VERT_CAP;
+
+// per-group shared memory (the hull staging area follows, 2 * hull_cap float4)
+struct EpaMem {
+    float4 fn[FCAP];       // face normal xyz, distance
+    uint32_t ft[FCAP];     // T0 | T1 << 8 | T2 << 16 | (valid + 2) << 24
+    float4 pv[VCAP];       // polytope vertices
+    uint16_t pab[VCAP];    // support index on A | on B << 8
+    uint8_t del[FCAP];     // faces deleted in this iteration, in index order
+};
+
+__device__ __forceinline__ int ft_v(uint32_t t, int k) { return (t >> (8 * k)) & 0xff; }
+__device__ __forceinline__ int ft_valid(uint32_t t) { return (int)(t >> 24) - 2; }
+__device__ __forceinline__ uint32_t ft_make(int a, int b, int c, int valid)
+{
+    return (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)c << 16) | ((uint32_t)(valid + 2) << 24);
+}
+
+template <int LPP>
+struct Group {
+    int lane;
+    unsigned mask;
+    __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+    __device__ __forceinline__ unsigned ballot(bool p) const
+    {
+        unsigned b = __ballot_sync(mask, p);
+        if (LPP < 32) b = (b & mask) >> (__ffs(mask) - 1);
+        return b;
+    }
+    __device__ __forceinline__ unsigned lt_mask() const { return (1u << lane) - 1u; }
+};
+
+// argmax of d.a over A and of (-d).b over B, first index on ties (.cu:55-101)
+template <int LPP>
+__device__ __forceinline__ void support(const Group<LPP>& g, const float4* hA, int nA, const float4* hB, int nB,
+                                        f3 d, f3& s, int& ia, int& ib)
+{
+    float bA = -1e30f, bB = -1e30f;
+    int iA = 0, iB = 0;
+    for (int i = g.lane; i < nA; i += LPP) {
+        float4 v = hA[i];
+        float t = d.x * v.x + d.y * v.y + d.z * v.z;
+        if (t > bA) { bA = t; iA = i; }
+    }
+    f3 nd = d * (-1.f);
+    for (int j = g.lane; j < nB; j += LPP) {
+        float4 v = hB[j];
+        float t = nd.x * v.x + nd.y * v.y + nd.z * v.z;
+        if (t > bB) { bB = t; iB = j; }
+    }
+#pragma unroll
+    for (int off = LPP / 2; off > 0; off >>= 1) {
+        float ov = __shfl_xor_sync(g.mask, bA, off, LPP);
+        int oi = __shfl_xor_sync(g.mask, iA, off, LPP);
+        if (ov > bA || (ov == bA && oi < iA)) { bA = ov; iA = oi; }
+        float ow = __shfl_xor_sync(g.mask, bB, off, LPP);
+        int oj = __shfl_xor_sync(g.mask, iB, off, LPP);
+        if (ow > bB || (ow == bB && oj < iB)) { bB = ow; iB = oj; }
+    }
+    ia = iA;
+    ib = iB;
+    float4 a = hA[iA], b = hB[iB];
+    s = mk3(a.x - b.x, a.y - b.y, a.z - b.z);
+}
+
+// ---- simplex tests, identical on every lane (.cu:103-268) ----
+__device__ __forceinline__ void seg_test(f3 P1, f3 P2, int& coll, f3& d)
+{
+    coll = -1;
+    d = mk3(0.f, 0.f, 0.f);
+    f3 e = P2 - P1;
+    if (dot(e, P2) < 0.f) { coll = 0; return; }
+    f3 t = cross(e, P2);
+    if (t.x == 0.f && t.y == 0.f && t.z == 0.f) { coll = 1; return; }
+    f3 tmp = cross(e, P2 * (-1.f));
+    d = cross(tmp, e);
+}
+
+__device__ __forceinline__ void tri_test(f3 P1, f3 P2, f3 P3, int& coll, f3& d)
+{
+    coll = -1;
+    d = mk3(0.f, 0.f, 0.f);
+    int c2, c3;
+    seg_test(P2, P3, c2, d);
+    if (c2 == 1) { coll = 1; return; }
+    seg_test(P1, P3, c3, d);
+    if (c3 == 1) { coll = 1; return; }
+    if (c2 + c3 > -1) { coll = 0; return; }
+    f3 e32 = P3 - P2, e13 = P1 - P3;
+    f3 n = cross(e32, e13);
+    f3 n2 = cross(e32, n);
+    f3 n3 = cross(e13, n);
+    if (dot(n2, P2) < 0.f) { d = n2; return; }
+    if (dot(n3, P3) < 0.f) { d = n3; return; }
+    if (dot(P3, n) == 0.f) { coll = 1; return; }
+    if (dot(n, P3) > 0.f) d = n * (-1.f);
+    else d = n;
+}
+
+__device__ __forceinline__ void tet_test(f3 P1, f3 P2, f3 P3, f3 P4, int& coll, f3& d, int& todel)
+{
+    coll = -1;
+    d = mk3(0.f, 0.f, 0.f);
+    todel = 0;
+    int c1, c2, c3;
+    tri_test(P1, P2, P4, c1, d);
+    if (c1 == 1) { coll = 1; return; }
+    tri_test(P2, P3, P4, c2, d);
+    if (c2 == 1) { coll = 1; return; }
+    tri_test(P3, P1, P4, c3, d);
+    if (c3 == 1) { coll = 1; return; }
+    if (c1 + c2 + c3 > -2) { coll = 0; return; }
+    f3 e13 = P1 - P3, e21 = P2 - P1, e32 = P3 - P2, e41 = P4 - P1;
+    f3 n2 = cross(e21, e41);
+    f3 e42 = P4 - P2;
+    f3 n3 = cross(e32, e42);
+    f3 e43 = P4 - P3;
+    f3 n4 = cross(e13, e43);
+    if (dot(n2, P4) < 0.f) { d = n2; todel = 3; }
+    else if (dot(n3, P4) < 0.f) { d = n3; todel = 1; }
+    else if (dot(n4, P4) < 0.f) { d = n4; todel = 2; }
+    else coll = 1;
+}
+
+// CorrectFlat: both determinants inside a double +-1e-6 window (.cu:256-268)
+__device__ __forceinline__ bool is_flat(f3 S1, f3 S2, f3 S3, f3 S4)
+{
+    float det1 = S1.x * (S2.y * S3.z - S3.y * S2.z) - S2.x * (S1.y * S3.z - S3.y * S1.z) + S3.x * (S1.y * S2.z - S2.y * S1.z);
+    if ((double)det1 < 0.000001 && (double)det1 > -0.000001) {
+        float det2 = S1.x * (S2.y * S4.z - S4.y * S2.z) - S2.x * (S1.y * S4.z - S4.y * S1.z) + S4.x * (S1.y * S2.z - S2.y * S1.z);
+        if ((double)det2 < 0.000001 && (double)det2 > -0.000001) return true;
+    }
+    return false;
+}
+
+// AddTriangle (.cu:270-325), one face per calling lane
+__device__ __forceinline__ void add_face(EpaMem& m, int e0, int e1, int e2, int f)
+{
+    f3 a = xyz(m.pv[e0]), b = xyz(m.pv[e1]), c = xyz(m.pv[e2]);
+    f3 n = cross(b - a, c - b);
+    float len = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
+    n = n / len;
+    float dist = dot(n, a);
+    int t1 = e1, t2 = e2;
+    if (dist < 0.f) {
+        t2 = e1;
+        t1 = e2;
+        dist = dist * (-1.f);
+        n = n * (-1.f);
+    }
+    f3 A = xyz(m.pv[e0]), B = xyz(m.pv[t1]), C = xyz(m.pv[t2]);
+    bool inside = false;
+    if (dot(cross(B - A, n), A * (-1.f)) < 0.f)
+        if (dot(cross(C - B, n), B * (-1.f)) < 0.f)
+            if (dot(cross(A - C, n), C * (-1.f)) < 0.f) inside = true;
+    int valid = 1;
+    if (!inside) {
+        valid = -2;
+        dist = 1e30f;
+    }
+    m.fn[f] = f4(n, dist);
+    m.ft[f] = ft_make(e0, t1, t2, valid);
+}
+
+// "x < best" of the reference's array_min_finder (.cu:41-53), NaN never wins
+__device__ __forceinline__ bool min_better(float v, int i, float bv, int bi)
+{
+    if (v != v) return false;
+    if (bv != bv) return true;
+    return v < bv || (v == bv && i < bi);
+}
+
+struct EpaResult {
+    float depth;
+    f3 n, cpA, cpB;
+    int fa[3], fb[3];
+    uint32_t status;
+};
+
+template <int LPP>
+__device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, const float4* hB, int nB,
+                    f3 S1, int a1, int b1, f3 S2, int a2, int b2, f3 S3, int a3, int b3, f3 S4, int a4, int b4,
+                    EpaResult& r)
+{
+    r.status = 0;
+    g.sync();
+    if (g.lane == 0) {
+        m.pv[0] = f4(S1, 0.f); m.pv[1] = f4(S2, 0.f); m.pv[2] = f4(S3, 0.f); m.pv[3] = f4(S4, 0.f);
+        m.pab[0] = (uint16_t)(a1 | (b1 << 8)); m.pab[1] = (uint16_t)(a2 | (b2 << 8));
+        m.pab[2] = (uint16_t)(a3 | (b3 << 8)); m.pab[3] = (uint16_t)(a4 | (b4 << 8));
+    }
+    g.sync();
+    if (g.lane < 4) {
+        const int e[4][3] = {{0, 1, 2}, {1, 2, 3}, {2, 0, 3}, {0, 1, 3}};
+        add_face(m, e[g.lane][0], e[g.lane][1], e[g.lane][2], g.lane);
+    }
+    g.sync();
+    int nt = 4, nv = 4, counter = 0, indmin = 0;
+    float xmin_old = 1e29f;
+    float proj = 2 * xmin_old + 1;
+    float xmin_new = 0.f;
+    while (xmin_old < proj) {
+        // first index of the minimum distance
+        float bv = __int_as_float(0x7fffffff);
+        int bi = 0x7fffffff;
+        for (int f = g.lane; f < nt; f += LPP) {
+            float v = m.fn[f].w;
+            if (min_better(v, f, bv, bi)) { bv = v; bi = f; }
+        }
+#pragma unroll
+        for (int off = LPP / 2; off > 0; off >>= 1) {
+            float ov = __shfl_xor_sync(g.mask, bv, off, LPP);
+            int oi = __shfl_xor_sync(g.mask, bi, off, LPP);
+            if (min_better(ov, oi, bv, bi)) { bv = ov; bi = oi; }
+        }
+        float d0 = m.fn[0].w;
+        indmin = (d0 != d0) ? 0 : bi;
+        float4 fm = m.fn[indmin];
+        xmin_new = fm.w;
+        xmin_old = xmin_new;
+        f3 n = xyz(fm);
+        f3 s;
+        int sa, sb;
+        support<LPP>(g, hA, nA, hB, nB, n, s, sa, sb);
+        proj = dot(n, s);
+        if (xmin_old > proj || ((double)xmin_old * 1.00001 > (double)proj && (double)xmin_old * 0.99999 < (double)proj)) break;
+        if (counter > 49) { r.status |= MWD_ST_EPA_NOCONV; break; }
+        counter = counter + 1;
+        if (nv >= VCAP) { r.status |= MWD_ST_EPA_OVERFLOW; break; }
+        g.sync();
+        if (g.lane == 0) {
+            m.pv[nv] = f4(s, 0.f);
+            m.pab[nv] = (uint16_t)(sa | (sb << 8));
+        }
+        nv++;
+        // visible faces -> deleted, collected in index order
+        int ndel = 0;
+        for (int base = 0; base < nt; base += LPP) {
+            int f = base + g.lane;
+            bool dead = false;
+            if (f < nt) {
+                uint32_t t = m.ft[f];
+                int vl = ft_valid(t);
+                if ((vl == 1 || vl == -2) && dot(s - xyz(m.pv[ft_v(t, 0)]), xyz(m.fn[f])) >= 0.f) {
+                    dead = true;
+                    m.ft[f] = (t & 0x00ffffffu) | ((uint32_t)(-1 + 2) << 24);
+                }
+            }
+            unsigned b = g.ballot(dead);
+            if (dead) m.del[ndel + __popc(b & g.lt_mask())] = (uint8_t)f;
+            ndel += __popc(b);
+        }
+        g.sync();
+        // horizon edges of the deleted faces, in face order then edge order (0,1),(1,2),(2,0);
+        // an edge is kept when fewer than two delpair increments land on it (.cu:482-544)
+        int nnew = 0;
+        bool overflow = false;
+        for (int base = 0; base < 3 * ndel; base += LPP) {
+            int c = base + g.lane;
+            bool keep = false;
+            int e0 = 0, e1 = 0;
+            if (c < 3 * ndel) {
+                uint32_t t = m.ft[m.del[c / 3]];
+                int k = c % 3;
+                e0 = ft_v(t, k);
+                e1 = ft_v(t, k == 2 ? 0 : k + 1);
+                int cnt = 0;
+                for (int j = 0; j < ndel; ++j) {
+                    uint32_t u = m.ft[m.del[j]];
+                    int x = ft_v(u, 0), y = ft_v(u, 1), z = ft_v(u, 2);
+                    cnt += (e0 == y && e1 == x) + (e0 == x && e1 == y) + (e0 == z && e1 == y) +
+                           (e0 == y && e1 == z) + (e0 == x && e1 == z) + (e0 == z && e1 == x);
+                }
+                keep = cnt < 2;
+            }
+            unsigned b = g.ballot(keep);
+            if (keep) {
+                int f = nt + nnew + __popc(b & g.lt_mask());
+                if (f < FCAP) add_face(m, e0, e1, nv - 1, f);
+            }
+            nnew += __popc(b);
+        }
+        if (nt + nnew > FCAP) overflow = true;
+        g.sync();
+        for (int k = g.lane; k < ndel; k += LPP) {
+            int f = m.del[k];
+            m.ft[f] = (m.ft[f] & 0x00ffffffu) | ((uint32_t)(0 + 2) << 24);
+            m.fn[f].w = 3e20f;
+        }
+        g.sync();
+        if (overflow) { r.status |= MWD_ST_EPA_OVERFLOW; break; }
+        nt += nnew;
+        counter = counter + 1;
+    }
+    g.sync();
+    r.depth = xmin_new;
+    uint32_t t = m.ft[indmin];
+    int a = ft_v(t, 0), b = ft_v(t, 1), c = ft_v(t, 2);
+    f3 n = xyz(m.fn[indmin]);
+    f3 Pr = n * r.depth;
+    f3 Va = xyz(m.pv[a]), Vb = xyz(m.pv[b]), Vc = xyz(m.pv[c]);
+    f3 v0 = Vb - Va, v1 = Vc - Va, v2 = Pr - Va;
+    if (dot(cross(v0, v1), n) < 0.f) {
+        v0 = Vc - Va;
+        v1 = Vb - Va;
+    }
+    float v00 = dot(v0, v0), v01 = dot(v0, v1), v11 = dot(v1, v1), v20 = dot(v2, v0), v21 = dot(v2, v1);
+    float den = v00 * v11 - v01 * v01;
+    float bv = (v11 * v20 - v01 * v21) / den;
+    float bw = (v00 * v21 - v01 * v20) / den;
+    float bu = (float)(1.0 - (double)bw - (double)bv);
+    int pa = m.pab[a], pb = m.pab[b], pc = m.pab[c];
+    r.fa[0] = pa & 0xff; r.fa[1] = pb & 0xff; r.fa[2] = pc & 0xff;
+    r.fb[0] = pa >> 8; r.fb[1] = pb >> 8; r.fb[2] = pc >> 8;
+    r.cpA = (xyz(hA[r.fa[0]]) * bu + xyz(hA[r.fa[1]]) * bv) + xyz(hA[r.fa[2]]) * bw;
+    r.cpB = (xyz(hB[r.fb[0]]) * bu + xyz(hB[r.fb[1]]) * bv) + xyz(hB[r.fb[2]]) * bw;
+    r.n = n;
+}
+
+struct ForceResult {
+    f3 F, TA, TB, dt;
+};
+
+// Force (.cu:647-871) with the pair-independent constants taken from mwd_material
+__device__ __forceinline__ void contact_force(f3 cA, f3 cB, float depth, f3 n, f3 cpA, f3 cpB, const mwd_material& M,
+                                              f3 vA, f3 vB, f3 wA, f3 wB, f3 dt, float4 qA, float dtn, float IsA,
+                                              float IsB, ForceResult& o)
+{
+    f3 cp = (cpA - cpB) / 2.f;
+    f3 dA = cp - cA, dB = cp - cB;
+    float dA2 = dA.x * dA.x + dA.y * dA.y + dA.z * dA.z;
+    float dB2 = dB.x * dB.x + dB.y * dB.y + dB.z * dB.z;
+    double C = M.inv_mu + (double)(dA2 / IsA) + (double)(dB2 / IsB);
+    float Kt = (float)(M.KtA * 1 / C);
+    float Gt = (float)((-1) * 2 / C * (double)M.ln_et);
+    if (dot(cB - cA, n) < 0.f) n = n * (-1.f);
+    float nn = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
+    n = n / nn;
+    f3 disp_n = n * depth;
+    f3 u = ((vA + cross(wA, cpA - cA)) - vB) - cross(wB, cpB - cB);
+    f3 un = n * dot(u, n);
+    f3 ut = u - un;
+    float utn = sqrtf(ut.x * ut.x + ut.y * ut.y + ut.z * ut.z);
+    f3 tij = mk3(0.f, 0.f, 0.f);
+    if (utn != 0.f) tij = ut / utn;
+    if (utn == 0.f && dtn != 0.f) tij = dt / dtn;
+    f3 Fn = (disp_n * (-1.f)) * M.Kn_f - un * M.Gn;
+    float Fnn = sqrtf(Fn.x * Fn.x + Fn.y * Fn.y + Fn.z * Fn.z);
+    f3 Ft = dt * (-1.f) * Kt - ut * Gt;
+    float Ftn = sqrtf(Ft.x * Ft.x + Ft.y * Ft.y + Ft.z * Ft.z);
+    // two separate tests as in the reference, so a NaN norm takes the second (slip) branch
+    if ((double)Ftn > M.mu * (double)Fnn) Ft = ((tij * Fnn) * (-1.f)) * M.mu_f;
+    if ((double)Ftn <= M.mu * (double)Fnn) {
+        float4 qi = qconj(qA);
+        o.dt = qtrip(qA, dt, qi) + ut * M.dt_f;
+    } else {
+        f3 t = (((tij * Fnn) * M.mu_f) * (-1.f)) - ut * Gt;
+        o.dt = (t * 1.f) / Kt;
+    }
+    f3 Ff = Ft + Fn;
+    o.F = Fn;
+    o.TA = cross(cp - cA, Ff);
+    o.TB = cross(cp - cB, Ff * (-1.f));
+}
+
+// ------------------------------------------------------------------ pair sources
+
+struct PairView {
+    f3 cA, cB, vA, vB, wA, wB, dt;
+    float4 qA;
+    float IsA, IsB, dtn;
+    int idA, idB, nA, nB;
+    int wall;
+};
+
+template <int MODE>
+__device__ __forceinline__ bool load_pair(const NarrowArgs& a, int64_t P, PairView& p, float4* hA, float4* hB,
+                                          int lane, int lpp)
+{
+    if (MODE == 0) {
+        const float* c;
+        c = a.A_com + 3 * P; p.cA = mk3(c[0], c[1], c[2]);
+        c = a.B_com + 3 * P; p.cB = mk3(c[0], c[1], c[2]);
+        c = a.A_vel + 3 * P; p.vA = mk3(c[0], c[1], c[2]);
+        c = a.B_vel + 3 * P; p.vB = mk3(c[0], c[1], c[2]);
+        c = a.A_w + 3 * P; p.wA = mk3(c[0], c[1], c[2]);
+        c = a.B_w + 3 * P; p.wB = mk3(c[0], c[1], c[2]);
+        c = a.qA + 4 * P; p.qA = make_float4(c[0], c[1], c[2], c[3]);
+        p.IsA = a.IsA[P];
+        p.IsB = a.IsB[P];
+        p.idA = a.A_id[P];
+        p.idB = a.B_id[P];
+        p.nA = a.A_nv[P];
+        p.nB = a.B_nv[P];
+        p.wall = (p.idA < a.n_wall || p.idB < a.n_wall) ? 1 : 0;
+        const int64_t hb = a.hist_mode ? 4 * P : P;
+        p.dt = mk3(a.hist_in[hb], a.hist_in[hb + 1], a.hist_in[hb + 2]);
+        if (p.nA < 0 || p.nB < 0 || p.nA > a.hull_cap || p.nB > a.hull_cap) return false;
+        const float* va = a.A_verts + P * a.V * 3;
+        const float* vb = a.B_verts + P * a.V * 3;
+        for (int i = lane; i < p.nA; i += lpp) hA[i] = make_float4(va[3 * i], va[3 * i + 1], va[3 * i + 2], 0.f);
+        for (int i = lane; i < p.nB; i += lpp) hB[i] = make_float4(vb[3 * i], vb[3 * i + 1], vb[3 * i + 2], 0.f);
+    } else {
+        int2 pr = reinterpret_cast<const int2*>(a.pairs)[P];
+        p.idA = pr.x;
+        p.idB = pr.y;
+        const double4 pa = reinterpret_cast<const double4*>(a.st.pos)[p.idA];
+        const double4 pb = reinterpret_cast<const double4*>(a.st.pos)[p.idB];
+        p.cA = mk3((float)pa.x, (float)pa.y, (float)pa.z);
+        p.cB = mk3((float)pb.x, (float)pb.y, (float)pb.z);
+        const float4* vel = reinterpret_cast<const float4*>(a.st.vel);
+        const float4* w = reinterpret_cast<const float4*>(a.st.w);
+        p.vA = xyz(vel[p.idA]);
+        p.vB = xyz(vel[p.idB]);
+        p.wA = xyz(w[p.idA]);
+        p.wB = xyz(w[p.idB]);
+        p.qA = reinterpret_cast<const float4*>(a.st.q)[p.idA];
+        p.IsA = reinterpret_cast<const float4*>(a.st.inertia)[p.idA].w;
+        p.IsB = reinterpret_cast<const float4*>(a.st.inertia)[p.idB].w;
+        p.wall = ((a.st.info[p.idA] | a.st.info[p.idB]) & 1);
+        p.dt = mk3(0.f, 0.f, 0.f);
+        const int oa = a.st.vert_off[p.idA], ob = a.st.vert_off[p.idB];
+        p.nA = a.st.vert_off[p.idA + 1] - oa;
+        p.nB = a.st.vert_off[p.idB + 1] - ob;
+        if (p.nA > a.hull_cap || p.nB > a.hull_cap) return false;
+        const float4* wv = reinterpret_cast<const float4*>(a.st.world_verts);
+        for (int i = lane; i < p.nA; i += lpp) hA[i] = wv[oa + i];
+        for (int i = lane; i < p.nB; i += lpp) hB[i] = wv[ob + i];
+    }
+    p.dtn = sqrtf(p.dt.x * p.dt.x + p.dt.y * p.dt.y + p.dt.z * p.dt.z);
+    return true;
+}
+
+template <int MODE>
+__device__ __forceinline__ void write_hist(const NarrowArgs& a, int64_t P, f3 v, float flag)
+{
+    if (MODE != 0) return;
+    if (a.hist_mode) {
+        float* h = a.hist_out + 4 * P;
+        h[0] = v.x; h[1] = v.y; h[2] = v.z; h[3] = flag;
+    } else {
+        reinterpret_cast<float4*>(a.hist_stage)[P] = make_float4(v.x, v.y, v.z, flag);
+        a.hist_wrote[P] = 1;
+    }
+}
+
+template <int MODE>
+__device__ __forceinline__ void accumulate(const NarrowArgs& a, const PairView& p, const ForceResult& fo)
+{
+    if (MODE == 0) {
+        atomicAdd(a.force + 3 * p.idA + 0, fo.F.x);
+        atomicAdd(a.force + 3 * p.idA + 1, fo.F.y);
+        atomicAdd(a.force + 3 * p.idA + 2, fo.F.z);
+        atomicAdd(a.force + 3 * p.idB + 0, -1 * fo.F.x);
+        atomicAdd(a.force + 3 * p.idB + 1, -1 * fo.F.y);
+        atomicAdd(a.force + 3 * p.idB + 2, -1 * fo.F.z);
+        atomicAdd(a.torque + 3 * p.idA + 0, fo.TA.x);
+        atomicAdd(a.torque + 3 * p.idA + 1, fo.TA.y);
+        atomicAdd(a.torque + 3 * p.idA + 2, fo.TA.z);
+        atomicAdd(a.torque + 3 * p.idB + 0, fo.TB.x);
+        atomicAdd(a.torque + 3 * p.idB + 1, fo.TB.y);
+        atomicAdd(a.torque + 3 * p.idB + 2, fo.TB.z);
+    } else {
+        float* F = a.st.force;
+        float* T = a.st.torque;
+        if (!(a.st.info[p.idA] & 1)) {
+            atomicAdd(F + 4 * p.idA + 0, fo.F.x);
+            atomicAdd(F + 4 * p.idA + 1, fo.F.y);
+            atomicAdd(F + 4 * p.idA + 2, fo.F.z);
+            atomicAdd(T + 4 * p.idA + 0, fo.TA.x);
+            atomicAdd(T + 4 * p.idA + 1, fo.TA.y);
+            atomicAdd(T + 4 * p.idA + 2, fo.TA.z);
+        }
+        if (!(a.st.info[p.idB] & 1)) {
+            atomicAdd(F + 4 * p.idB + 0, -1 * fo.F.x);
+            atomicAdd(F + 4 * p.idB + 1, -1 * fo.F.y);
+            atomicAdd(F + 4 * p.idB + 2, -1 * fo.F.z);
+            atomicAdd(T + 4 * p.idB + 0, fo.TB.x);
+            atomicAdd(T + 4 * p.idB + 1, fo.TB.y);
+            atomicAdd(T + 4 * p.idB + 2, fo.TB.z);
+        }
+    }
+}
+
+template <int LPP, int MODE>
+__device__ void process_pair(const NarrowArgs& a, int64_t P, const Group<LPP>& g, EpaMem& em, float4* hA, float4* hB)
+{
+    PairView p;
+    const bool ok = load_pair<MODE>(a, P, p, hA, hB, g.lane, LPP);
+    g.sync();
+    const bool leader = g.lane == 0;
+    if (!ok) {
+        if (leader) {
+            set_status(a.status, MWD_ST_BAD_SHAPE);
+            if (a.collision) a.collision[P] = -1;
+        }
+        return;
+    }
+    const mwd_material& M = MODE == 0 ? a.mat[p.wall] : a.scenes[a.st.info[p.idA] >> 1].mat[p.wall];
+
+    f3 S1, S2, S3, S4, d3, d4;
+    int a1, b1, a2, b2, a3, b3, a4 = 0, b4 = 0, todel = 0, coll = -1;
+    bool early = false, resolved = false;
+    f3 d1 = p.cB - p.cA;
+    support<LPP>(g, hA, p.nA, hB, p.nB, d1, S1, a1, b1);
+    if (dot(d1, S1) < 0.f) early = true;
+    if (!early) {
+        f3 d2 = d1 * (-1.f);
+        support<LPP>(g, hA, p.nA, hB, p.nB, d2, S2, a2, b2);
+        if (dot(d2, S2) < 0.f) early = true;
+    }
+    if (!early) {
+        seg_test(S1, S2, coll, d3);
+        if (coll == 0) early = true;
+    }
+    if (!early) {
+        support<LPP>(g, hA, p.nA, hB, p.nB, d3, S3, a3, b3);
+        if (dot(d3, S3) < 0.f) early = true;
+    }
+    if (!early) {
+        tri_test(S1, S2, S3, coll, d4);
+        if (coll == 0) early = true;
+    }
+    ForceResult fo;
+    fo.F = fo.TA = fo.TB = mk3(0.f, 0.f, 0.f);
+    fo.dt = p.dt;
+    EpaResult er;
+    er.status = 0;
+    uint32_t st = 0;
+    if (!early) {
+        int zz = 0;
+        while (zz < 50) {
+            support<LPP>(g, hA, p.nA, hB, p.nB, d4, S4, a4, b4);
+            if (dot(d4, S4) < 0.f) { early = true; break; }
+            bool hit = false;
+            if (S4.x == 0.f && S4.y == 0.f && S4.z == 0.f) hit = true;
+            else {
+                tet_test(S1, S2, S3, S4, coll, d4, todel);
+                if (coll == 0) { early = true; break; }
+                if (coll == 1) hit = true;
+            }
+            if (hit) {
+                if (is_flat(S1, S2, S3, S4)) {
+                    d4 = cross(S1, S2);
+                    support<LPP>(g, hA, p.nA, hB, p.nB, d4, S4, a4, b4);
+                }
+                epa<LPP>(g, em, hA, p.nA, hB, p.nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er);
+                contact_force(p.cA, p.cB, er.depth, er.n, er.cpA, er.cpB, M, p.vA, p.vB, p.wA, p.wB, p.dt, p.qA,
+                              p.dtn, p.IsA, p.IsB, fo);
+                st |= er.status;
+                resolved = true;
+                break;
+            }
+            f3 n1, n2, n3;
+            int na1, nb1, na2, nb2, na3, nb3;
+            if (todel == 1) { n1 = S2; na1 = a2; nb1 = b2; n2 = S3; na2 = a3; nb2 = b3; n3 = S4; na3 = a4; nb3 = b4; }
+            else if (todel == 2) { n1 = S3; na1 = a3; nb1 = b3; n2 = S1; na2 = a1; nb2 = b1; n3 = S4; na3 = a4; nb3 = b4; }
+            else { n1 = S1; na1 = a1; nb1 = b1; n2 = S2; na2 = a2; nb2 = b2; n3 = S4; na3 = a4; nb3 = b4; }
+            S1 = n1; a1 = na1; b1 = nb1; S2 = n2; a2 = na2; b2 = nb2; S3 = n3; a3 = na3; b3 = nb3;
+            zz = zz + 1;
+        }
+        if (!early && !resolved) st |= MWD_ST_GJK_NOCONV;
+    }
+    if (!leader) return;
+    set_status(a.status, st);
+    if (early) {
+        if (a.collision) a.collision[P] = 0;
+        write_hist<MODE>(a, P, mk3(0.f, 0.f, 0.f), 0.f);
+    } else {
+        if (a.collision) a.collision[P] = resolved ? 1 : -1;
+        if (resolved) write_hist<MODE>(a, P, fo.dt, 1.f);
+        accumulate<MODE>(a, p, fo);
+    }
+    if (a.diag) {
+        float* dg = a.diag + 10 * P;
+        if (resolved) {
+            dg[0] = er.depth;
+            dg[1] = er.n.x; dg[2] = er.n.y; dg[3] = er.n.z;
+            dg[4] = er.cpA.x; dg[5] = er.cpA.y; dg[6] = er.cpA.z;
+            dg[7] = er.cpB.x; dg[8] = er.cpB.y; dg[9] = er.cpB.z;
+        } else {
+            for (int k = 0; k < 10; ++k) dg[k] = 0.f;
+        }
+    }
+    if (a.face_ids) {
+        int* fid = a.face_ids + 6 * P;
+        for (int k = 0; k < 3; ++k) {
+            fid[k] = resolved ? er.fa[k] : -1;
+            fid[3 + k] = resolved ? er.fb[k] : -1;
+        }
+    }
+}
+
+template <int LPP, int MODE>
+__global__ void __launch_bounds__(NARROW_THREADS) narrow_kernel(NarrowArgs a)
+{
+    extern __shared__ float4 smem[];
+    constexpr int GPB = NARROW_THREADS / LPP;
+    const int grp = threadIdx.x / LPP;
+    Group<LPP> g;
+    g.lane = threadIdx.x % LPP;
+    g.mask = LPP == 32 ? 0xffffffffu : (((1u << LPP) - 1u) << ((threadIdx.x & 31) / LPP * LPP));
+    EpaMem* em = reinterpret_cast<EpaMem*>(smem) + grp;
+    float4* hull = reinterpret_cast<float4*>(reinterpret_cast<EpaMem*>(smem) + GPB) + (size_t)grp * 2 * a.hull_cap;
+    float4* hA = hull;
+    float4* hB = hull + a.hull_cap;
+    int64_t n = a.n_pairs;
+    if (MODE == 1) {
+        int64_t m = *a.n_pairs_dev;
+        n = m < a.pair_cap ? m : a.pair_cap;
+    }
+    for (int64_t P = (int64_t)blockIdx.x * GPB + grp; P < n; P += (int64_t)gridDim.x * GPB) {
+        process_pair<LPP, MODE>(a, P, g, *em, hA, hB);
+        g.sync();
+    }
+}
+
+// Resolve the reference's overlapping stride-1 history writes (.cu:1018-1021, :1158-1161): the
+// value left at hist[k] is the one written by the highest pair index P' in [k-3, k] that wrote.
+__global__ void hist_resolve_kernel(float* hist, const float4* stage, const uint8_t* wrote, int64_t n)
+{
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n + 3) return;
+    for (int64_t P = (k < n - 1 ? k : n - 1); P >= 0 && P >= k - 3; --P) {
+        if (wrote[P]) {
+            float4 v = stage[P];
+            int j = (int)(k - P);
+            hist[k] = j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w;
+            return;
+        }
+    }
+}
+
+template <int LPP, int MODE>
+int launch_lpp(const NarrowArgs& a, int64_t n_hint, cudaStream_t s)
+{
+    constexpr int GPB = NARROW_THREADS / LPP;
+    size_t shm = (size_t)GPB * sizeof(EpaMem) + (size_t)GPB * 2 * a.hull_cap * sizeof(float4);
+    static bool attr_set = false;
+    if (!attr_set) {
+        MWD_CUDA(cudaFuncSetAttribute(narrow_kernel<LPP, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        attr_set = true;
+    }
+    int per_sm = 0;
+    MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, narrow_kernel<LPP, MODE>, NARROW_THREADS, shm));
+    if (per_sm < 1) per_sm = 1;
+    int64_t grid = (int64_t)num_sms() * per_sm;
+    int64_t need = (n_hint + GPB - 1) / GPB;
+    if (n_hint >= 0 && need < grid) grid = need > 0 ? need : 1;
+    narrow_kernel<LPP, MODE><<<(unsigned)grid, NARROW_THREADS, shm, s>>>(a);
+    MWD_CUDA(cudaGetLastError());
+    return MWD_OK;
+}
+
+}  // namespace
+
+size_t narrow_smem_bytes(int lpp, int hull_cap)
+{
+    int gpb = NARROW_THREADS / lpp;
+    return (size_t)gpb * sizeof(EpaMem) + (size_t)gpb * 2 * hull_cap * sizeof(float4);
+}
+
+int launch_narrow(const NarrowArgs& a, int mode, int lanes, int64_t n_hint, cudaStream_t s)
+{
+    if (mode == 0) {
+        switch (lanes) {
+            case 4: return launch_lpp<4, 0>(a, n_hint, s);
+            case 8: return launch_lpp<8, 0>(a, n_hint, s);
+            case 16: return launch_lpp<16, 0>(a, n_hint, s);
+            case 32: return launch_lpp<32, 0>(a, n_hint, s);
+        }
+    } else {
+        switch (lanes) {
+            case 4: return launch_lpp<4, 1>(a, n_hint, s);
+            case 8: return launch_lpp<8, 1>(a, n_hint, s);
+            case 16: return launch_lpp<16, 1>(a, n_hint, s);
+            case 32: return launch_lpp<32, 1>(a, n_hint, s);
+        }
+    }
+    set_error("lanes per pair must be 4, 8, 16 or 32 (got %d)", lanes);
+    return MWD_ERR_INVALID;
+}
+
+int launch_hist_resolve(float* hist, const float* stage, const uint8_t* wrote, int64_t n, cudaStream_t s)
+{
+    if (n <= 0) return MWD_OK;
+    int64_t total = n + 3;
+    unsigned grid = (unsigned)((total + 255) / 256);
+    hist_resolve_kernel<<<grid, 256, 0, s>>>(hist, reinterpret_cast<const float4*>(stage), wrote, n);
+    MWD_CUDA(cudaGetLastError());
+    return MWD_OK;
+}
+
+}  // namespace mwd

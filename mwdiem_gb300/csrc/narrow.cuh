@@ -1,0 +1,45 @@
+// Launch arguments of the narrow-phase kernel (internal to libmwdem).
+#pragma once
+
+#include "common.cuh"
+
+namespace mwd {
+
+constexpr int NARROW_THREADS = 128;
+
+struct NarrowArgs {
+    // mode 0: per-pair arrays in the reference's layout
+    const float *A_com, *B_com, *A_verts, *B_verts, *A_vel, *B_vel, *A_w, *B_w, *qA, *qB, *IsA, *IsB;
+    const int32_t *A_nv, *B_nv, *A_id, *B_id;
+    const float* hist_in;   // history as read by the pairs
+    float* hist_out;        // stride-4 mode: written in place
+    float* hist_stage;      // stride-1 mode: (P,4) staging of each pair's four writes
+    uint8_t* hist_wrote;    // stride-1 mode: (P,) 1 when the pair wrote
+    float* force;           // (N,3)
+    float* torque;          // (N,3)
+    int32_t V;
+    int32_t n_wall;
+    int32_t hist_mode;
+    int32_t pad0;
+    int64_t n_pairs;
+    mwd_material mat[2];
+    // mode 1: particle tables
+    mwd_state st;
+    const mwd_scene* scenes;
+    const int32_t* pairs;
+    const int64_t* n_pairs_dev;
+    int64_t pair_cap;
+    // common
+    int32_t* collision;     // optional
+    float* diag;            // optional (P,10)
+    int32_t* face_ids;      // optional (P,6): support indices of the final EPA face, A then B
+    uint32_t* status;       // optional
+    int32_t hull_cap;       // hull vertices staged per side
+    int32_t pad1;
+};
+
+int launch_narrow(const NarrowArgs& a, int mode, int lanes, int64_t n_hint, cudaStream_t s);
+int launch_hist_resolve(float* hist, const float* stage, const uint8_t* wrote, int64_t n, cudaStream_t s);
+size_t narrow_smem_bytes(int lpp, int hull_cap);
+
+}  // namespace mwd

@@ -1,0 +1,64 @@
+"""Broad phase on the GPU against the oracle's restatement of ``Linked_cell_hash`` (whose list is
+identical to the reference's, test_oracle.py) and of the wall test / cell keys of MWDiem.py:808-816.
+Bar: the same set of oriented pairs, bit-exact keys."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def pairset(p):
+    return set(map(tuple, np.asarray(p).reshape(-1, 2).tolist()))
+
+
+@pytest.mark.parametrize("seed,n,spread", [(0, 20000, 20.0), (1, 5000, 4.0), (2, 3000, 60.0)])
+def test_linked_cell_hash_matches(seed, n, spread):
+    from mwdiem_gb300 import LIBRARY_Coarse_contact_detection as CCD
+    rng = np.random.default_rng(seed)
+    W = 5
+    com = np.zeros((n + W, 3))
+    com[W:] = rng.uniform([-spread, -spread, -3], [spread, spread, 3 * spread], size=(n, 3))
+    cs, nx, ny = 2.4, 17, 17
+    keys_o = oracle.cell_keys(com, cs, cs, cs, nx, ny)
+    keys_g = CCD.cell_keys(com, cs, cs, cs, nx, ny)
+    assert np.array_equal(keys_o, keys_g)
+    ref = oracle.linked_cell_hash(W, n + W, keys_o, nx, ny)
+    got = CCD.Linked_cell_hash(None, nx, ny, W, n + W, [], keys_g)
+    assert len(got) == len(ref)
+    assert pairset(got) == pairset(ref)
+
+
+def test_crowded_cells_and_negative_keys():
+    from mwdiem_gb300 import LIBRARY_Coarse_contact_detection as CCD
+    rng = np.random.default_rng(3)
+    n = 4000
+    com = rng.normal(scale=3.0, size=(n, 3))  # many particles per cell, negative coordinates
+    keys = oracle.cell_keys(com, 2.0, 2.0, 2.0, 7, 7)
+    ref = oracle.linked_cell_hash(0, n, keys, 7, 7)
+    got = CCD.Linked_cell_hash(None, 7, 7, 0, n, [], keys)
+    assert pairset(got) == pairset(ref) and len(got) == len(ref)
+
+
+def test_wall_pairs_match():
+    from mwdiem_gb300 import LIBRARY_Coarse_contact_detection as CCD
+    rng = np.random.default_rng(4)
+    W, n = 5, 6000
+    com = rng.uniform(-20, 20, size=(n + W, 3))
+    wn = rng.normal(size=(W, 3))
+    wn /= np.linalg.norm(wn, axis=1, keepdims=True)
+    wc = rng.uniform(-5, 5, size=(W, 3))
+    ref = oracle.wall_pairs(W, W, n + W, com, wn, wc, 14.4)
+    got = CCD.wall_pairs(com, wn, wc, W, W, n + W, 14.4).cpu().numpy()
+    assert np.array_equal(got, ref)  # wall-major order, as MWDiem.py:808-811
+
+
+def test_empty_ranges():
+    from mwdiem_gb300 import LIBRARY_Coarse_contact_detection as CCD
+    keys = np.zeros(10, np.int64)
+    assert CCD.Linked_cell_hash(None, 4, 4, 3, 3, [], keys) == []
+    one = CCD.Linked_cell_hash(None, 4, 4, 3, 4, [], keys)
+    assert one == []
+    two = CCD.Linked_cell_hash(None, 4, 4, 3, 5, [], keys)
+    assert pairset(two) == pairset(oracle.linked_cell_hash(3, 5, keys, 4, 4))

@@ -1,0 +1,45 @@
+"""The C-ABI library builds, loads and exports every entry point include/mwdem.h declares (no
+device calls: this runs without a GPU)."""
+import re
+from pathlib import Path
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "mwdem.h"
+
+
+def declared():
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    return sorted(set(re.findall(r"\b(mwd_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    from mwdiem_gb300 import _lib
+    h = _lib.lib()
+    names = declared()
+    assert len(names) >= 14
+    for n in names:
+        assert hasattr(h, n), n
+    assert set(_lib.EXPORTED) <= set(names)
+    assert h.mwd_version() >= 1
+
+
+def test_host_side_material_constants():
+    import ctypes
+    import math
+    from mwdiem_gb300 import _lib
+    p = _lib.ContactParams(1e5, 0.372, 0.372, 0.5, 3e4, 0.5, 0.6, 0.3, 5e-5, 4, 0, 0, 0)
+    m = (_lib.Material * 2)()
+    _lib.check(_lib.lib().mwd_derive_material(ctypes.byref(p), m))
+    # Gn = -2 mu / tc * ln(en) with tc = sqrt(mu (pi^2 + ln^2 en) / Kn): = 2 zeta sqrt(mu Kn)-like
+    ln = math.log(0.372)
+    tc = math.sqrt(0.5 * (math.pi ** 2 + ln * ln) / 1e5)
+    assert abs(m[0].Gn - (-2 * 0.5 / tc * ln)) < 1e-3 * abs(m[0].Gn)
+    assert abs(m[1].inv_mu - 1 / 0.3) < 1e-12
+    assert m[0].Kn_f == 1e5 and abs(m[0].dt_f - 5e-5) < 1e-10
+
+
+def test_errors_are_codes_not_aborts():
+    import ctypes
+    from mwdiem_gb300 import _lib
+    rc = _lib.lib().mwd_contact_pairs(-1, 8, 1, *([None] * 20), None, None, None, None)
+    assert rc == _lib.MWD_ERR_INVALID
+    assert b"bad arguments" in _lib.lib().mwd_last_error()
