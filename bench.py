@@ -1,0 +1,332 @@
+#!/usr/bin/env python
+"""Benchmark: device-resident DEM steps of the 20,000-hull pour on one GB300 (particle-steps/s).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One step = broad phase + narrow phase + contact force + integrator over the whole scene (one CUDA
+graph replay).  The scene fits in L2 (~20 MB of state), so L2 is flushed (a 256 MB write) before
+every timed step; each step is timed with CUDA events on the stream it runs on and the times are
+summed.  `e2e` is the same step through the public host-buffer API (state copied from pinned host
+memory to the device and back every step).  `roofline` covers the kernel that dominates the step.
+`--impl reference` times the reference's own CPU path (oracle/stepper.py: its kernels compiled
+for the host from their source when that build is available, else the oracle's restatement) on
+this machine's host cores, on the same scene.  Under torchrun every rank runs an independent
+replica (the scene does not shard; no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT, ROOT / "oracle", ROOT / "tests"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+N_PARTICLES = 20000
+SCENE = dict(n=N_PARTICLES, seed=0, box=40.0, spacing=2.6, jitter=0.1, n_min=12, n_max=32, r_min=0.8, r_max=1.2,
+             zeta=0.3, kn=1e5, mu=0.5, dt=5e-5)
+WORKLOAD = ("pour20k: 20,000 convex hulls of U{12..32} points on a sphere of radius U[0.8,1.2], jittered "
+            "lattice (spacing 2.6) in a 40x40 box, random orientations, at rest, gravity; kn 1e5, damping "
+            "ratio 0.3 (en=et=0.372), mu 0.5, dt 5e-5")
+METRIC = "particle-steps/s"
+KERNELS_PER_STEP = 14  # broad phase 12 (assign, 3 scan, scatter, order, crowded, count, 3 scan, emit) + narrow + integrate
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--lanes", type=int, default=8)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-breakdown", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_scene(seed):
+    from mwdiem_gb300 import scene
+    p = dict(SCENE, seed=seed)
+    return scene.pour_scene(**p)
+
+
+def ref_kind(spec, V):
+    """The reference path on the host: its kernels compiled from their own source when that build is
+    available for this scene ('reference'), else the oracle's restatement ('port')."""
+    import stepper
+    try:
+        return stepper.RefStepper(spec, V=V, kind="reference", nthreads=os.cpu_count() or 1), "reference"
+    except Exception:
+        return stepper.RefStepper(spec, V=V, kind="port", nthreads=1), "port"
+
+
+def cpu_path_rate(spec, max_seconds=20.0, max_steps=5):
+    """Particle-steps/s of the reference path on the host (bounded sample: whole steps of the scene)."""
+    s, kind = ref_kind(spec, None)
+    n = spec.n_particles
+    s.step()  # warm-up (allocations, library load)
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps:
+        s.step()
+        steps += 1
+        if time.perf_counter() - t0 > max_seconds:
+            break
+    dt = time.perf_counter() - t0
+    cores = (os.cpu_count() or 1) if kind == "reference" else 1
+    return {"value": n * steps / dt, "unit": METRIC, "cores": cores, "kind": kind,
+            "sample": f"{steps} full steps of the {n}-particle pour after 1 warm-up step"}, s
+
+
+def narrow_flops(sim):
+    """Algorithmic FP32 operations of one narrow-phase launch on the current pair list, counted by
+    the kernel itself (work counters on): 5 per vertex per support query (3 multiplies + 2 adds of
+    the dot product) plus ~60 per EPA face built (cross product, normalisation, inside test)."""
+    dots, faces, queries = sim.count_narrow_work()
+    return 5.0 * dots + 60.0 * faces, dict(vertex_dots=dots, epa_faces=faces, support_queries=queries)
+
+
+def integrate_bytes(sim):
+    # per row: reads pos, dx_all (2 x 32 B), 14 float4 (224 B), info + vert_off (8 B);
+    # writes pos, dx_all (64 B), 9 float4 state + 2 zeroed accumulators (176 B); per vertex 16 B in, 16 B out
+    return sim.n * (64 + 224 + 8 + 64 + 176) + sim.state.n_verts * 32
+
+
+def main():
+    args = parse()
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        return reference_arm(args)
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from mwdiem_gb300 import _lib
+    from mwdiem_gb300.sim import Simulator
+
+    spec = build_scene(seed=SCENE["seed"] + rank)
+    sim = Simulator(spec, lanes=args.lanes)
+    V = sim.max_verts
+    sim.capture(steps_per_replay=1)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    for _ in range(max(3, args.warmup)):
+        sim.replay(1)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        sim.replay(1)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    status = sim.check_status()
+    n_pairs = sim.n_pairs()
+    value = N_PARTICLES * args.steps * world / (total_ms * 1e-3)
+
+    # e2e: state from pinned host memory in, result back out, every step
+    host = sim.host_state()
+    nbytes = sim.host_state_bytes()
+    sim.step_host(host, 1)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ne = max(1, args.e2e_steps)
+    e0.record(stream)
+    for _ in range(ne):
+        sim.step_host(host, 1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    te = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e = {"value": N_PARTICLES * ne * world / (float(te.item()) * 1e-3), "unit": METRIC,
+           "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "particles": N_PARTICLES, "walls": spec.n_walls,
+                       "candidate_pairs_per_step": n_pairs, "lanes_per_pair": args.lanes, "cuda_graph": True,
+                       "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
+            "e2e": e2e, "gpu_launches": KERNELS_PER_STEP * args.steps, "clocks": clk,
+            "status": _lib.status_names(status)}
+
+    if rank == 0 and not args.no_breakdown:
+        line["breakdown"], line["roofline"] = breakdown(sim, V, flush)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cb, _ = cpu_path_rate(build_scene(SCENE["seed"]))
+            line["cpu_baseline"] = cb
+        except Exception as e:  # report, do not fail the GPU measurement
+            line["cpu_baseline"] = {"error": str(e)[:200]}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def breakdown(sim, V, flush, reps=10):
+    """Per-stage device time (CUDA events on the launching stream, L2 flushed before each stage's
+    step) and the roofline of the dominant stage."""
+    import torch
+    from mwdiem_gb300 import _lib
+    stream = torch.cuda.current_stream()
+    acc = {"broad": 0.0, "narrow": 0.0, "integrate": 0.0}
+    for _ in range(reps):
+        flush.zero_()
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        evs[0].record(stream)
+        sim.broadphase()
+        evs[1].record(stream)
+        sim.narrow_force()
+        evs[2].record(stream)
+        sim.integrate()
+        evs[3].record(stream)
+        torch.cuda.synchronize()
+        acc["broad"] += evs[0].elapsed_time(evs[1])
+        acc["narrow"] += evs[1].elapsed_time(evs[2])
+        acc["integrate"] += evs[2].elapsed_time(evs[3])
+    ms = {k: v / reps for k, v in acc.items()}
+    pk = peaks()
+    import ctypes as C
+    scratch = torch.zeros(8 * 1024, dtype=torch.float32, device="cuda")
+    tf = C.c_double(0)
+    _lib.check(_lib.lib().mwd_probe_fp32(20000, scratch.data_ptr(), C.byref(tf), None))
+    fp32_peak = tf.value
+    flops, work = narrow_flops(sim)
+    ib = integrate_bytes(sim)
+    out = {"ms": ms, "n_pairs": sim.n_pairs(), "narrow_fp32_tflops": flops / (ms["narrow"] * 1e-3) / 1e12,
+           "narrow_fp32_peak_tflops_measured": fp32_peak,
+           "integrate_gbs": ib / (ms["integrate"] * 1e-3) / 1e9, "narrow_work": work}
+    dom = max(ms, key=ms.get)
+    if dom == "narrow":
+        a = flops / (ms["narrow"] * 1e-3) / 1e12
+        roof = {"kernel": "narrow_kernel<8,1>", "bound": "fp32", "achieved": a, "peak": fp32_peak,
+                "unit": "TFLOP/s", "frac": a / fp32_peak if fp32_peak else None, "traffic": None,
+                "peak_source": "measured in this run (mwd_probe_fp32: FMUL+FADD chains, no FMA)"}
+    elif dom == "integrate":
+        hbm = pk.get("hbm_gbs", 6800.0)
+        a = ib / (ms["integrate"] * 1e-3) / 1e9
+        roof = {"kernel": "integrate_kernel", "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s",
+                "frac": a / hbm, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in pk else "fallback 6800"}
+    else:
+        hbm = pk.get("hbm_gbs", 6800.0)
+        n, P = sim.n, sim.n_pairs()
+        bbytes = n * (32 + 4 + 4 + 4 + 4 + 4 + 8) + sim.total_cells * 12 + P * (8 + 8 + 8)
+        a = bbytes / (ms["broad"] * 1e-3) / 1e9
+        roof = {"kernel": "broad phase (12 kernels)", "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s",
+                "frac": a / hbm, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in pk else "fallback 6800"}
+    return out, roof
+
+
+def reference_arm(args):
+    """The reference's CPU path on this host, same scene, same metric."""
+    spec = build_scene(SCENE["seed"])
+    s, kind = ref_kind(spec, None)
+    cores = (os.cpu_count() or 1) if kind == "reference" else 1
+    for _ in range(max(0, args.warmup)):
+        s.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.step()
+    dt = time.perf_counter() - t0
+    value = spec.n_particles * args.steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "particles": spec.n_particles, "walls": spec.n_walls,
+                       "path": "wall test + cell keys + Linked_cell_hash (C restatement) -> per-pair gather -> "
+                               "contact kernel (FP32) -> Verlet kernel (FP64)"},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": kind,
+                             "sample": f"{args.steps} full steps of the {spec.n_particles}-particle pour"},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

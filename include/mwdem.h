@@ -46,7 +46,7 @@ enum {
 #define MWD_EPA_FACE_CAP 128   /* append-only EPA face list per pair */
 #define MWD_EPA_VERT_CAP 32    /* EPA polytope vertices per pair (4 + 25 iterations + 1) */
 #define MWD_HULL_CAP 64        /* hull vertices per side staged in shared memory */
-#define MWD_CELL_CAP 32        /* members per cell handled by the CPython set-order emulation */
+#define MWD_CELL_CAP 306       /* members per cell handled by the CPython set-order emulation */
 
 /* ------------------------------------------------------------------------------------------
  * Contact law.  The reference bakes these into its kernel source as literals
@@ -215,6 +215,11 @@ typedef struct {
     int64_t* n_pairs;      /* (1,) candidate count of the last broad phase */
     uint32_t* status;      /* (1,) status word */
     int32_t* collision;    /* (pair_cap,) optional contact flags (NULL to skip) */
+    int32_t* crowded;      /* (crowded_cap,) cells with more than 32 members (set order by a warp) */
+    int32_t* n_crowded;    /* (1,) zero on entry, left zero on exit */
+    int64_t crowded_cap;   /* n / 33 + 1 is always enough */
+    uint64_t* work_counters; /* optional (3,), added to by the narrow phase: vertex dot products of the
+                              support queries, EPA faces created, support queries (NULL: not counted) */
     int64_t total_cells;
     int64_t pair_cap;
 } mwd_work;
@@ -237,6 +242,11 @@ int mwd_integrate(mwd_state* st, const mwd_scene* scenes_dev, uint32_t* status, 
 /* broad phase + narrow phase + integrator, n_steps times. */
 int mwd_step(mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes_host, int32_t n_scenes,
              mwd_work* work, int32_t lanes, int32_t n_steps, mwd_stream_t stream);
+
+/* FP32 issue-rate probe (multiply and add chains, no FMA): runs iters x 16 FLOP per thread on
+ * 8 x SM-count blocks of 256 threads, times it with CUDA events (synchronises the stream) and
+ * writes the rate in TFLOP/s.  scratch: >= 8 x SM-count floats.  The narrow phase's roofline. */
+int mwd_probe_fp32(int32_t iters, float* scratch, double* tflops_out /* host */, mwd_stream_t stream);
 
 /* Library information. */
 const char* mwd_last_error(void);

@@ -28,7 +28,7 @@ ST_BAD_SHAPE = 64
 EPA_FACE_CAP = 128
 EPA_VERT_CAP = 32
 HULL_CAP = 64
-CELL_CAP = 32
+CELL_CAP = 306
 
 STATUS_NAMES = {ST_EPA_NOCONV: "EPA_NOCONV", ST_EPA_OVERFLOW: "EPA_OVERFLOW", ST_GJK_NOCONV: "GJK_NOCONV",
                 ST_PAIR_OVERFLOW: "PAIR_OVERFLOW", ST_CELL_RANGE: "CELL_RANGE", ST_CELL_CROWDED: "CELL_CROWDED",
@@ -78,8 +78,9 @@ class Scene(C.Structure):
 
 class Work(C.Structure):
     _fields_ = [(n, _P) for n in ("cell_count", "cell_start", "cell_of", "sorted", "pair_count", "pairs",
-                                  "scan_tmp", "n_pairs", "status", "collision")] + \
-               [("total_cells", C.c_int64), ("pair_cap", C.c_int64)]
+                                  "scan_tmp", "n_pairs", "status", "collision", "crowded", "n_crowded")] + \
+               [("crowded_cap", C.c_int64), ("work_counters", _P), ("total_cells", C.c_int64),
+                ("pair_cap", C.c_int64)]
 
 
 _lock = threading.Lock()
@@ -112,6 +113,7 @@ def lib():
             "mwd_narrow_force": (C.c_int, [C.POINTER(State), _P, C.POINTER(Work), i32, _P]),
             "mwd_integrate": (C.c_int, [C.POINTER(State), _P, _P, _P]),
             "mwd_step": (C.c_int, [C.POINTER(State), _P, _P, i32, C.POINTER(Work), i32, i32, _P]),
+            "mwd_probe_fp32": (C.c_int, [i32, _P, C.POINTER(C.c_double), _P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(h, name)
@@ -123,7 +125,7 @@ def lib():
 
 EXPORTED = ("mwd_last_error", "mwd_version", "mwd_num_sms", "mwd_scan_tmp_ints", "mwd_derive_material",
             "mwd_contact_pairs", "mwd_verlet_ref", "mwd_cell_keys", "mwd_wall_pairs", "mwd_linked_cell_hash",
-            "mwd_broadphase", "mwd_narrow_force", "mwd_integrate", "mwd_step")
+            "mwd_broadphase", "mwd_narrow_force", "mwd_integrate", "mwd_step", "mwd_probe_fp32")
 
 
 def check(rc: int):

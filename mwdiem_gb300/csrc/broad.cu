@@ -121,14 +121,12 @@ __global__ void scan_final_kernel(const int32_t* in, int64_t n, const int32_t* b
 // list(set) would list them in CPython 3.12: open addressing on hash(i) = i, up to 9 linear probes
 // when they fit below the mask, then perturbation (perturb >>= 5; i = 5 i + 1 + perturb), table of
 // 8 slots grown to the next power of two above 4*used when fill*5 >= mask*3.
-__device__ void pyset_order(const int* m, int k, int* out)
+template <unsigned TABCAP>
+__device__ bool pyset_order(const int* m, int k, int* out, int* tab, unsigned char* used, int* tmp,
+                            unsigned char* used2)
 {
-    int tab[128];
-    unsigned char used[128];
-    int tmp[128];
-    unsigned char used2[128];
     unsigned mask = 7;
-    for (int s = 0; s < 128; ++s) used[s] = 0;
+    for (int s = 0; s < 8; ++s) used[s] = 0;
     int fill = 0;
     for (int e = 0; e < k; ++e) {
         const uint64_t h = (uint64_t)(uint32_t)m[e];
@@ -153,6 +151,7 @@ __device__ void pyset_order(const int* m, int k, int* out)
         if ((unsigned)fill * 5u >= mask * 3u) {
             unsigned newsize = 8, minused = (unsigned)fill * 4u;
             while (newsize <= minused) newsize <<= 1;
+            if (newsize > TABCAP) return false;
             unsigned newmask = newsize - 1;
             for (unsigned s = 0; s < newsize; ++s) used2[s] = 0;
             for (unsigned s = 0; s <= mask; ++s) {
@@ -183,7 +182,15 @@ __device__ void pyset_order(const int* m, int k, int* out)
     int c = 0;
     for (unsigned s = 0; s <= mask; ++s)
         if (used[s]) out[c++] = tab[s];
+    return true;
 }
+
+// cells up to SMALL_CELL members are ordered by one thread with the table in local memory; larger
+// cells go to a list handled by one warp each with the table in shared memory
+constexpr int SMALL_CELL = 32;
+constexpr int SMALL_TAB = 128;   // table size CPython reaches for <= 32 members
+constexpr int BIG_TAB = 512;     // ... for <= 306 members
+constexpr int BIG_CELL = 306;
 
 // ---------------------------------------------------------------- broad-phase kernels
 
@@ -249,17 +256,13 @@ __global__ void order_kernel(BroadArgs a)
     }
     for (int j = s; j < e; ++j)
         if (a.scatter_out[j] < r) return;  // the smallest id of the cell orders it
-    if (k > MWD_CELL_CAP) {
-        set_status(a.status, MWD_ST_CELL_CROWDED);
-        // ascending ids (selection by rank; cells this crowded are pathological)
-        for (int j = s; j < e; ++j) {
-            int v = a.scatter_out[j], rank = 0;
-            for (int i = s; i < e; ++i) rank += a.scatter_out[i] < v;
-            a.sorted[s + rank] = v;
-        }
+    if (k > SMALL_CELL) {
+        const int idx = atomicAdd(a.n_crowded, 1);
+        if (idx < a.crowded_cap) a.crowded[idx] = g;
+        else set_status(a.status, MWD_ST_CELL_CROWDED);
         return;
     }
-    int m[MWD_CELL_CAP];
+    int m[SMALL_CELL];
     for (int j = 0; j < k; ++j) {
         int v = a.scatter_out[s + j];
         int i = j;
@@ -269,15 +272,55 @@ __global__ void order_kernel(BroadArgs a)
         }
         m[i] = v;
     }
-    int o[MWD_CELL_CAP];
-    pyset_order(m, k, o);
+    int o[SMALL_CELL];
+    int tab[SMALL_TAB], tmp[SMALL_TAB];
+    unsigned char used[SMALL_TAB], used2[SMALL_TAB];
+    pyset_order<SMALL_TAB>(m, k, o, tab, used, tmp, used2);
     for (int j = 0; j < k; ++j) a.sorted[s + j] = o[j];
+}
+
+// one warp per crowded cell: members ranked by id in parallel, then lane 0 replays the set inserts
+__global__ void __launch_bounds__(32) order_crowded_kernel(BroadArgs a)
+{
+    __shared__ int m[BIG_CELL];
+    __shared__ int o[BIG_CELL];
+    __shared__ int tab[BIG_TAB], tmp[BIG_TAB];
+    __shared__ unsigned char used[BIG_TAB], used2[BIG_TAB];
+    const int64_t nc = *a.n_crowded;
+    const int n = (int)(nc < a.crowded_cap ? nc : a.crowded_cap);
+    for (int c = blockIdx.x; c < n; c += gridDim.x) {
+        const int g = a.crowded[c];
+        const int s = a.cell_start[g], e = a.cell_start[g + 1];
+        const int k = e - s;
+        if (k > BIG_CELL) {
+            // beyond the emulated table size: ascending ids, flagged
+            for (int j = threadIdx.x; j < k; j += 32) {
+                int v = a.scatter_out[s + j], rank = 0;
+                for (int i = 0; i < k; ++i) rank += a.scatter_out[s + i] < v;
+                a.sorted[s + rank] = v;
+            }
+            if (threadIdx.x == 0) set_status(a.status, MWD_ST_CELL_CROWDED);
+            __syncwarp();
+            continue;
+        }
+        for (int j = threadIdx.x; j < k; j += 32) {
+            int v = a.scatter_out[s + j], rank = 0;
+            for (int i = 0; i < k; ++i) rank += a.scatter_out[s + i] < v;
+            m[rank] = v;
+        }
+        __syncwarp();
+        if (threadIdx.x == 0) pyset_order<BIG_TAB>(m, k, o, tab, used, tmp, used2);
+        __syncwarp();
+        for (int j = threadIdx.x; j < k; j += 32) a.sorted[s + j] = o[j];
+        __syncwarp();
+    }
 }
 
 template <bool EMIT>
 __global__ void pairs_kernel(BroadArgs a)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!EMIT && t == 0) *a.n_crowded = 0;  // consumed by the crowded-cell pass, which ran before
     const int n_sorted = a.cell_start[a.total_cells];
     if (t >= n_sorted) {
         if (!EMIT && t < a.row_hi - a.row_lo) a.pair_count[t] = 0;
@@ -418,6 +461,7 @@ int launch_broad(const BroadArgs& a, cudaStream_t s)
     if (rc) return rc;
     scatter_kernel<<<blocks(rows, T), T, 0, s>>>(a);
     order_kernel<<<blocks(rows, T), T, 0, s>>>(a);
+    order_crowded_kernel<<<(unsigned)(a.crowded_cap < 1024 ? (a.crowded_cap > 0 ? a.crowded_cap : 1) : 1024), 32, 0, s>>>(a);
     // rows that have a cell are at most `rows`; threads past cell_start[total] exit
     pairs_kernel<false><<<blocks(rows, T), T, 0, s>>>(a);
     rc = launch_scan(a.pair_count, rows, a.pair_count, a.scan_tmp, a.n_pairs, a.pair_cap, a.status,

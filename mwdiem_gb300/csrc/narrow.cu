@@ -62,10 +62,17 @@ struct Group {
 };
 
 // argmax of d.a over A and of (-d).b over B, first index on ties (.cu:55-101)
+// work counted per pair when the caller asks for it: vertex dot products, EPA faces, support queries
+struct Work3 {
+    uint32_t dots, faces, queries;
+};
+
 template <int LPP>
 __device__ __forceinline__ void support(const Group<LPP>& g, const float4* hA, int nA, const float4* hB, int nB,
-                                        f3 d, f3& s, int& ia, int& ib)
+                                        f3 d, f3& s, int& ia, int& ib, Work3& wk)
 {
+    wk.dots += (uint32_t)(nA + nB);
+    wk.queries += 1;
     float bA = -1e30f, bB = -1e30f;
     int iA = 0, iB = 0;
     for (int i = g.lane; i < nA; i += LPP) {
@@ -211,7 +218,7 @@ struct EpaResult {
 template <int LPP>
 __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, const float4* hB, int nB,
                     f3 S1, int a1, int b1, f3 S2, int a2, int b2, f3 S3, int a3, int b3, f3 S4, int a4, int b4,
-                    EpaResult& r)
+                    EpaResult& r, Work3& wk)
 {
     r.status = 0;
     g.sync();
@@ -226,6 +233,7 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
         add_face(m, e[g.lane][0], e[g.lane][1], e[g.lane][2], g.lane);
     }
     g.sync();
+    wk.faces += 4;
     int nt = 4, nv = 4, counter = 0, indmin = 0;
     float xmin_old = 1e29f;
     float proj = 2 * xmin_old + 1;
@@ -252,7 +260,7 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
         f3 n = xyz(fm);
         f3 s;
         int sa, sb;
-        support<LPP>(g, hA, nA, hB, nB, n, s, sa, sb);
+        support<LPP>(g, hA, nA, hB, nB, n, s, sa, sb, wk);
         proj = dot(n, s);
         if (xmin_old > proj || ((double)xmin_old * 1.00001 > (double)proj && (double)xmin_old * 0.99999 < (double)proj)) break;
         if (counter > 49) { r.status |= MWD_ST_EPA_NOCONV; break; }
@@ -321,6 +329,7 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
         g.sync();
         if (overflow) { r.status |= MWD_ST_EPA_OVERFLOW; break; }
         nt += nnew;
+        wk.faces += (uint32_t)nnew;
         counter = counter + 1;
     }
     g.sync();
@@ -529,15 +538,16 @@ __device__ void process_pair(const NarrowArgs& a, int64_t P, const Group<LPP>& g
     }
     const mwd_material& M = MODE == 0 ? a.mat[p.wall] : a.scenes[a.st.info[p.idA] >> 1].mat[p.wall];
 
+    Work3 wk = {0u, 0u, 0u};
     f3 S1, S2, S3, S4, d3, d4;
     int a1, b1, a2, b2, a3, b3, a4 = 0, b4 = 0, todel = 0, coll = -1;
     bool early = false, resolved = false;
     f3 d1 = p.cB - p.cA;
-    support<LPP>(g, hA, p.nA, hB, p.nB, d1, S1, a1, b1);
+    support<LPP>(g, hA, p.nA, hB, p.nB, d1, S1, a1, b1, wk);
     if (dot(d1, S1) < 0.f) early = true;
     if (!early) {
         f3 d2 = d1 * (-1.f);
-        support<LPP>(g, hA, p.nA, hB, p.nB, d2, S2, a2, b2);
+        support<LPP>(g, hA, p.nA, hB, p.nB, d2, S2, a2, b2, wk);
         if (dot(d2, S2) < 0.f) early = true;
     }
     if (!early) {
@@ -545,7 +555,7 @@ __device__ void process_pair(const NarrowArgs& a, int64_t P, const Group<LPP>& g
         if (coll == 0) early = true;
     }
     if (!early) {
-        support<LPP>(g, hA, p.nA, hB, p.nB, d3, S3, a3, b3);
+        support<LPP>(g, hA, p.nA, hB, p.nB, d3, S3, a3, b3, wk);
         if (dot(d3, S3) < 0.f) early = true;
     }
     if (!early) {
@@ -561,7 +571,7 @@ __device__ void process_pair(const NarrowArgs& a, int64_t P, const Group<LPP>& g
     if (!early) {
         int zz = 0;
         while (zz < 50) {
-            support<LPP>(g, hA, p.nA, hB, p.nB, d4, S4, a4, b4);
+            support<LPP>(g, hA, p.nA, hB, p.nB, d4, S4, a4, b4, wk);
             if (dot(d4, S4) < 0.f) { early = true; break; }
             bool hit = false;
             if (S4.x == 0.f && S4.y == 0.f && S4.z == 0.f) hit = true;
@@ -573,9 +583,9 @@ __device__ void process_pair(const NarrowArgs& a, int64_t P, const Group<LPP>& g
             if (hit) {
                 if (is_flat(S1, S2, S3, S4)) {
                     d4 = cross(S1, S2);
-                    support<LPP>(g, hA, p.nA, hB, p.nB, d4, S4, a4, b4);
+                    support<LPP>(g, hA, p.nA, hB, p.nB, d4, S4, a4, b4, wk);
                 }
-                epa<LPP>(g, em, hA, p.nA, hB, p.nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er);
+                epa<LPP>(g, em, hA, p.nA, hB, p.nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er, wk);
                 contact_force(p.cA, p.cB, er.depth, er.n, er.cpA, er.cpB, M, p.vA, p.vB, p.wA, p.wB, p.dt, p.qA,
                               p.dtn, p.IsA, p.IsB, fo);
                 st |= er.status;
@@ -594,6 +604,11 @@ __device__ void process_pair(const NarrowArgs& a, int64_t P, const Group<LPP>& g
     }
     if (!leader) return;
     set_status(a.status, st);
+    if (a.work_counters) {
+        atomicAdd(a.work_counters + 0, (unsigned long long)wk.dots);
+        atomicAdd(a.work_counters + 1, (unsigned long long)wk.faces);
+        atomicAdd(a.work_counters + 2, (unsigned long long)wk.queries);
+    }
     if (early) {
         if (a.collision) a.collision[P] = 0;
         write_hist<MODE>(a, P, mk3(0.f, 0.f, 0.f), 0.f);
@@ -667,14 +682,22 @@ int launch_lpp(const NarrowArgs& a, int64_t n_hint, cudaStream_t s)
 {
     constexpr int GPB = NARROW_THREADS / LPP;
     size_t shm = (size_t)GPB * sizeof(EpaMem) + (size_t)GPB * 2 * a.hull_cap * sizeof(float4);
+    // attribute and occupancy are queried once per shared-memory size, so that launches made
+    // during CUDA-graph capture issue no other runtime calls
     static bool attr_set = false;
+    static size_t cached_shm = 0;
+    static int cached_per_sm = 0;
     if (!attr_set) {
         MWD_CUDA(cudaFuncSetAttribute(narrow_kernel<LPP, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         attr_set = true;
     }
-    int per_sm = 0;
-    MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, narrow_kernel<LPP, MODE>, NARROW_THREADS, shm));
-    if (per_sm < 1) per_sm = 1;
+    if (shm != cached_shm || cached_per_sm == 0) {
+        int per_sm = 0;
+        MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, narrow_kernel<LPP, MODE>, NARROW_THREADS, shm));
+        cached_per_sm = per_sm < 1 ? 1 : per_sm;
+        cached_shm = shm;
+    }
+    const int per_sm = cached_per_sm;
     int64_t grid = (int64_t)num_sms() * per_sm;
     int64_t need = (n_hint + GPB - 1) / GPB;
     if (n_hint >= 0 && need < grid) grid = need > 0 ? need : 1;

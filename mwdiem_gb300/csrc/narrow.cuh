@@ -34,6 +34,7 @@ struct NarrowArgs {
     float* diag;            // optional (P,10)
     int32_t* face_ids;      // optional (P,6): support indices of the final EPA face, A then B
     uint32_t* status;       // optional
+    unsigned long long* work_counters;  // optional (3,): vertex dot products, EPA faces, support queries
     int32_t hull_cap;       // hull vertices staged per side
     int32_t pad1;
 };

@@ -27,7 +27,27 @@ def register_verlet(params: dict):
         VERLET_SETS.append(dict(params))
 
 
+def pour_sets(n=20000, box=40.0, spacing=2.6, r_max=1.2, zeta=0.3, kn=1e5, mu=0.5, dt=5e-5, V=32):
+    """Contact and integrator parameter sets of the pour scene (the benchmark workload), computed
+    from its sizes alone with the same code that builds the scene."""
+    from mwdiem_gb300 import scene
+    walls = scene.pour_walls(n, box, spacing, r_max)
+    sp = scene.SceneSpec(walls=walls)
+    en = scene.restitution_from_damping(zeta)
+    W = len(walls)
+    box6 = sp.box()
+    c = dict(Kn=kn, en=en, et=en, mu=mu, Kn_wall=kn, en_wall=en, et_wall=en, mu_wall=mu, num_vertices_max=V,
+             num_particles_wall=W, timestep=dt)
+    v = dict(timestep_size=dt, num_particles=n + W, num_vertices_max=V, syssize_x_max=box6[0],
+             syssize_x_min=box6[1], syssize_y_max=box6[2], syssize_y_min=box6[3], syssize_z_max=box6[4],
+             syssize_z_min=box6[5], num_part_min=W, num_part_max=n + W)
+    return c, v
+
+
 def render_all():
+    c, v = pour_sets()
+    register_contact(c)
+    register_verlet(v)
     out = []
     for p in CONTACT_SETS:
         out.append(build_ref.ensure_built("contact", p, "f32"))

@@ -62,3 +62,22 @@ def test_empty_ranges():
     assert one == []
     two = CCD.Linked_cell_hash(None, 4, 4, 3, 5, [], keys)
     assert pairset(two) == pairset(oracle.linked_cell_hash(3, 5, keys, 4, 4))
+
+
+def test_very_crowded_cell_flags_status():
+    # more members in one cell than the set-order emulation covers: same unordered pairs, status set
+    import torch
+    from mwdiem_gb300 import _lib
+    n = 400
+    keys = np.zeros(n, np.int64)
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    pairs = torch.zeros((n * n, 2), dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
+    k = torch.from_numpy(keys).cuda()
+    _lib.check(_lib.lib().mwd_linked_cell_hash(0, n, k.data_ptr(), 4, 4, pairs.data_ptr(), n * n, cnt.data_ptr(),
+                                               st.data_ptr(), None))
+    torch.cuda.synchronize()
+    got = pairs[: int(cnt.item())].cpu().numpy()
+    ref = oracle.linked_cell_hash(0, n, keys, 4, 4)
+    assert int(st.item()) & _lib.ST_CELL_CROWDED
+    assert set(map(frozenset, got.tolist())) == set(map(frozenset, ref.tolist()))

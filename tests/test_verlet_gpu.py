@@ -35,9 +35,18 @@ def test_verlet_matches_oracle_fp64():
     for k in ("v", "v12", "w12bf", "wbf", "w", "com", "dxall", "q12", "q", "qall", "verts"):
         scale = max(np.abs(a[k]).max(), 1e-30)
         assert np.abs(a[k] - b[k]).max() <= 1e-12 * scale, k
-    # rows outside [n_min, n_max) untouched, the fly-away row reset (zero velocity)
+    # rows outside [n_min, n_max) untouched
     assert np.array_equal(b["com"][:W], st["com"][:W])
-    assert np.all(b["v"][W + 1] == 0)
+
+
+def test_verlet_fly_away_reset():
+    # gpu_Verlet.cu:338-352: a centre leaving the box stops the particle and undoes the move
+    N, V, W, dt = 16, 8, 3, 1e-3
+    st, box = make_verlet_state(N, V, seed=6, W=W)
+    b = {k: v.copy() for k, v in st.items()}
+    gpu_step(b, dt, box, W, N, V)
+    assert np.all(b["v"][W + 1] == 0) and np.all(b["v12"][W + 1] == 0) and np.all(b["w"][W + 1] == 0)
+    assert np.allclose(b["com"][W + 1], st["com"][W + 1], rtol=0, atol=1e-12)
 
 
 def test_verlet_device_tensors():
