@@ -121,15 +121,17 @@ __global__ void scan_final_kernel(const int32_t* in, int64_t n, const int32_t* b
 // list(set) would list them in CPython 3.12: open addressing on hash(i) = i, up to 9 linear probes
 // when they fit below the mask, then perturbation (perturb >>= 5; i = 5 i + 1 + perturb), table of
 // 8 slots grown to the next power of two above 4*used when fill*5 >= mask*3.
+// ids are hashed as (row - base): the particle number inside its own scene, which is what the
+// reference hashes (each scene's particles are numbered from 0)
 template <unsigned TABCAP>
 __device__ bool pyset_order(const int* m, int k, int* out, int* tab, unsigned char* used, int* tmp,
-                            unsigned char* used2)
+                            unsigned char* used2, int base)
 {
     unsigned mask = 7;
     for (int s = 0; s < 8; ++s) used[s] = 0;
     int fill = 0;
     for (int e = 0; e < k; ++e) {
-        const uint64_t h = (uint64_t)(uint32_t)m[e];
+        const uint64_t h = (uint64_t)(uint32_t)(m[e] - base);
         unsigned i = (unsigned)(h & mask);
         uint64_t perturb = h;
         for (;;) {
@@ -156,7 +158,7 @@ __device__ bool pyset_order(const int* m, int k, int* out, int* tab, unsigned ch
             for (unsigned s = 0; s < newsize; ++s) used2[s] = 0;
             for (unsigned s = 0; s <= mask; ++s) {
                 if (!used[s]) continue;
-                const uint64_t hh = (uint64_t)(uint32_t)tab[s];
+                const uint64_t hh = (uint64_t)(uint32_t)(tab[s] - base);
                 unsigned ii = (unsigned)(hh & newmask);
                 uint64_t pp = hh;
                 for (;;) {
@@ -275,7 +277,8 @@ __global__ void order_kernel(BroadArgs a)
     int o[SMALL_CELL];
     int tab[SMALL_TAB], tmp[SMALL_TAB];
     unsigned char used[SMALL_TAB], used2[SMALL_TAB];
-    pyset_order<SMALL_TAB>(m, k, o, tab, used, tmp, used2);
+    const int base = a.info ? a.scenes[scene_of(a, r)].row_begin : 0;
+    pyset_order<SMALL_TAB>(m, k, o, tab, used, tmp, used2, base);
     for (int j = 0; j < k; ++j) a.sorted[s + j] = o[j];
 }
 
@@ -309,7 +312,8 @@ __global__ void __launch_bounds__(32) order_crowded_kernel(BroadArgs a)
             m[rank] = v;
         }
         __syncwarp();
-        if (threadIdx.x == 0) pyset_order<BIG_TAB>(m, k, o, tab, used, tmp, used2);
+        const int base = a.info ? a.scenes[scene_of(a, m[0])].row_begin : 0;
+        if (threadIdx.x == 0) pyset_order<BIG_TAB>(m, k, o, tab, used, tmp, used2, base);
         __syncwarp();
         for (int j = threadIdx.x; j < k; j += 32) a.sorted[s + j] = o[j];
         __syncwarp();
