@@ -162,7 +162,7 @@ int mwd_linked_cell_hash(int32_t n_lo, int32_t n_hi, const int64_t* keys, int64_
  * ------------------------------------------------------------------------------------------ */
 typedef struct {
     /* per particle row (n rows) */
-    double* pos;         /* (n,4) centre of mass, FP64 */
+    double* pos;         /* (n,4) centre of mass, FP64; .w = bounding radius (largest |r0|) of the row */
     double* dx_all;      /* (n,4) displacement accumulated since the last host sync */
     float* vel;          /* (n,4) v */
     float* vel_half;     /* (n,4) v_1/2 */

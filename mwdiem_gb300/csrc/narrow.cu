@@ -655,6 +655,39 @@ __global__ void __launch_bounds__(NARROW_THREADS) narrow_kernel(NarrowArgs a)
         int64_t m = *a.n_pairs_dev;
         n = m < a.pair_cap ? m : a.pair_cap;
     }
+    if (MODE == 1) {
+        // Sphere pre-test, LPP candidate pairs at a time (one per lane).  pos.w holds each row's
+        // bounding radius (largest vertex distance from the centre).  When the centres are farther
+        // apart than rA + rB plus a rounding margin, the reference's first GJK test,
+        // d.(a* - b*) < 0 with d = cB - cA (gpu_fine_contact_detection.cu:1010-1023), is negative:
+        // d.a* <= d.cA + |d| rA and -d.b* <= -d.cB + |d| rB give d.(a* - b*) <= -|d| (|d| - rA - rB).
+        // Such pairs get the reference's outcome (collision 0, no force) without running GJK.
+        const double4* pos = reinterpret_cast<const double4*>(a.st.pos);
+        const int2* pairs = reinterpret_cast<const int2*>(a.pairs);
+        const int64_t stride = (int64_t)gridDim.x * GPB * LPP;
+        for (int64_t base = ((int64_t)blockIdx.x * GPB + grp) * LPP; base < n; base += stride) {
+            const int64_t Pl = base + g.lane;
+            bool live = false;
+            if (Pl < n) {
+                const int2 pr = pairs[Pl];
+                const double4 pa = pos[pr.x], pb = pos[pr.y];
+                const float dx = (float)(pb.x - pa.x), dy = (float)(pb.y - pa.y), dz = (float)(pb.z - pa.z);
+                const float mag = fmaxf(fmaxf(fabsf((float)pa.x), fabsf((float)pa.y)), fabsf((float)pa.z)) +
+                                  fmaxf(fmaxf(fabsf((float)pb.x), fabsf((float)pb.y)), fabsf((float)pb.z));
+                const float r = (float)(pa.w + pb.w) * 1.001f + 1e-5f * mag + 1e-6f;
+                live = dx * dx + dy * dy + dz * dz <= r * r;
+                if (!live && a.collision) a.collision[Pl] = 0;
+            }
+            unsigned m = g.ballot(live);
+            while (m) {
+                const int l = __ffs(m) - 1;
+                m &= m - 1;
+                process_pair<LPP, MODE>(a, base + l, g, *em, hA, hB);
+                g.sync();
+            }
+        }
+        return;
+    }
     for (int64_t P = (int64_t)blockIdx.x * GPB + grp; P < n; P += (int64_t)gridDim.x * GPB) {
         process_pair<LPP, MODE>(a, P, g, *em, hA, hB);
         g.sync();

@@ -100,6 +100,8 @@ class Simulator:
         bv[:, :3] = np.concatenate(verts, 0)
         pos = np.zeros((n, 4))
         pos[:, :3] = np.asarray(rows_pos)
+        # bounding radius of each row (used by the narrow phase's sphere pre-test)
+        pos[:, 3] = [float(np.sqrt((v.astype(np.float32).astype(np.float64) ** 2).sum(1)).max()) for v in verts]
         f32 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(self.device)  # noqa: E731
         f64 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(self.device)  # noqa: E731
         z4 = np.zeros((n, 4))
