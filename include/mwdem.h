@@ -105,6 +105,26 @@ int mwd_contact_pairs(int64_t n_pairs, int32_t V, int32_t n_particles,
                       const mwd_contact_params* prm /* host */, float* diag, uint32_t* status,
                       mwd_stream_t stream);
 
+/* The same narrow phase + contact force as mwd_contact_pairs, same arguments and results, for
+ * callers that cannot allocate device memory: code running while a CUDA stream is being captured
+ * (an allocation would break the capture), host frameworks that own every device allocation, and
+ * processes with a fixed memory budget.  No counterpart in the reference (which allocates and
+ * copies on every call).  Its scratch (17 bytes per pair, for the stride-1 history staging) is a
+ * fixed array compiled into the library: at most MWD_NOALLOC_MAX_PAIRS pairs per call (larger calls
+ * return MWD_ERR_INVALID); every GPU that loads the library holds the array (~4.5 MB) until the
+ * process exits; all calls share it, so calls that overlap on the GPU race and must be ordered by
+ * the caller.  The first call on a device looks up the array's address with that device current;
+ * make that first call before any stream capture.  Calls no allocating routine. */
+#define MWD_NOALLOC_MAX_PAIRS (1 << 18)
+int mwd_contact_pairs_noalloc(int64_t n_pairs, int32_t V, int32_t n_particles,
+                              const float* A_com, const float* B_com, const float* A_verts, const float* B_verts,
+                              const float* A_vel, const float* B_vel, const float* A_angvel, const float* B_angvel,
+                              const int32_t* A_nv, const int32_t* B_nv, const int32_t* A_id, const int32_t* B_id,
+                              float* hist, float* force, float* torque, const float* qA, const float* qB,
+                              const float* IsA, const float* IsB, int32_t* collision,
+                              const mwd_contact_params* prm /* host */, float* diag, uint32_t* status,
+                              mwd_stream_t stream);
+
 /* ------------------------------------------------------------------------------------------
  * Integrator over the reference's FP64 arrays.
  * Replaces gpu_Verlet.gpu_Verlett / Verlet (LIBRARIES/gpu_Verlet.py:18-50, gpu_Verlet.cu:85-431).

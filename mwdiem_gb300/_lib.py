@@ -29,6 +29,7 @@ EPA_FACE_CAP = 128
 EPA_VERT_CAP = 32
 HULL_CAP = 64
 CELL_CAP = 306
+NOALLOC_MAX_PAIRS = 1 << 18
 
 STATUS_NAMES = {ST_EPA_NOCONV: "EPA_NOCONV", ST_EPA_OVERFLOW: "EPA_OVERFLOW", ST_GJK_NOCONV: "GJK_NOCONV",
                 ST_PAIR_OVERFLOW: "PAIR_OVERFLOW", ST_CELL_RANGE: "CELL_RANGE", ST_CELL_CROWDED: "CELL_CROWDED",
@@ -114,6 +115,8 @@ def lib():
             "mwd_integrate": (C.c_int, [C.POINTER(State), _P, _P, _P]),
             "mwd_step": (C.c_int, [C.POINTER(State), _P, _P, i32, C.POINTER(Work), i32, i32, _P]),
             "mwd_probe_fp32": (C.c_int, [i32, _P, C.POINTER(C.c_double), _P]),
+            "mwd_contact_pairs_noalloc": (C.c_int, [i64, i32, i32] + [_P] * 20 +
+                                          [C.POINTER(ContactParams), _P, _P, _P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(h, name)
@@ -125,7 +128,8 @@ def lib():
 
 EXPORTED = ("mwd_last_error", "mwd_version", "mwd_num_sms", "mwd_scan_tmp_ints", "mwd_derive_material",
             "mwd_contact_pairs", "mwd_verlet_ref", "mwd_cell_keys", "mwd_wall_pairs", "mwd_linked_cell_hash",
-            "mwd_broadphase", "mwd_narrow_force", "mwd_integrate", "mwd_step", "mwd_probe_fp32")
+            "mwd_broadphase", "mwd_narrow_force", "mwd_integrate", "mwd_step", "mwd_probe_fp32",
+            "mwd_contact_pairs_noalloc")
 
 
 def check(rc: int):
