@@ -240,6 +240,9 @@ typedef struct {
     int64_t crowded_cap;   /* n / 33 + 1 is always enough */
     uint64_t* work_counters; /* optional (3,), added to by the narrow phase: vertex dot products of the
                               support queries, EPA faces created, support queries (NULL: not counted) */
+    int32_t* epa_count;    /* (1,) two-pass narrow phase: pairs found in contact by the GJK pass */
+    void* epa_rec;         /* (epa_cap, 80 B): their simplex; NULL selects the single-pass kernel */
+    int64_t epa_cap;
     int64_t total_cells;
     int64_t pair_cap;
 } mwd_work;

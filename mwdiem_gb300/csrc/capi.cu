@@ -421,6 +421,12 @@ int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work*
     a.status = work->status;
     a.work_counters = reinterpret_cast<unsigned long long*>(work->work_counters);
     a.hull_cap = st->max_verts;
+    if (work->epa_rec && work->epa_count && work->epa_cap > 0) {
+        a.epa_count = work->epa_count;
+        a.epa_rec = work->epa_rec;
+        a.epa_cap = work->epa_cap;
+        return launch_narrow_two_pass(a, lp, reinterpret_cast<cudaStream_t>(stream));
+    }
     return launch_narrow(a, 1, lp, -1, reinterpret_cast<cudaStream_t>(stream));
 }
 

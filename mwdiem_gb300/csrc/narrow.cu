@@ -694,6 +694,229 @@ __global__ void __launch_bounds__(NARROW_THREADS) narrow_kernel(NarrowArgs a)
     }
 }
 
+// ------------------------------------------------------------------ two-pass narrow phase (table mode)
+//
+// Pass 1 (gjk_pass_kernel) runs the sphere pre-test and GJK on every candidate pair with the hulls
+// read straight from the world-vertex table (no shared memory, few registers, many resident warps);
+// separated and undecided pairs are finished there.  Pairs GJK finds in contact append the simplex
+// it stopped on to a compact list.  Pass 2 (epa_pass_kernel) continues exactly where pass 1
+// stopped -- CorrectFlat, EPA, force -- for the listed pairs only, with the shared-memory polytope.
+// The operation sequence per pair is the single-pass kernel's.
+
+struct SimplexRec {
+    float4 S[4];     // simplex points (w unused)
+    int64_t P;       // pair index
+    uint32_t ia;     // support indices on A, 8 bits each
+    uint32_t ib;     // support indices on B
+};
+
+// GJK up to the decision (.cu:996-1288): 0 separated, 1 in contact (simplex in rec), -1 undecided
+// after 50 tetrahedron iterations.
+template <int LPP>
+__device__ int gjk_decide(const Group<LPP>& g, const float4* hA, int nA, const float4* hB, int nB, f3 cA, f3 cB,
+                          SimplexRec& rec, Work3& wk)
+{
+    f3 S1, S2, S3, S4, d3, d4;
+    int a1, b1, a2, b2, a3, b3, a4 = 0, b4 = 0, todel = 0, coll = -1;
+    f3 d1 = cB - cA;
+    support<LPP>(g, hA, nA, hB, nB, d1, S1, a1, b1, wk);
+    if (dot(d1, S1) < 0.f) return 0;
+    f3 d2 = d1 * (-1.f);
+    support<LPP>(g, hA, nA, hB, nB, d2, S2, a2, b2, wk);
+    if (dot(d2, S2) < 0.f) return 0;
+    seg_test(S1, S2, coll, d3);
+    if (coll == 0) return 0;
+    support<LPP>(g, hA, nA, hB, nB, d3, S3, a3, b3, wk);
+    if (dot(d3, S3) < 0.f) return 0;
+    tri_test(S1, S2, S3, coll, d4);
+    if (coll == 0) return 0;
+    for (int zz = 0; zz < 50; ++zz) {
+        support<LPP>(g, hA, nA, hB, nB, d4, S4, a4, b4, wk);
+        if (dot(d4, S4) < 0.f) return 0;
+        bool hit = false;
+        if (S4.x == 0.f && S4.y == 0.f && S4.z == 0.f) hit = true;
+        else {
+            tet_test(S1, S2, S3, S4, coll, d4, todel);
+            if (coll == 0) return 0;
+            if (coll == 1) hit = true;
+        }
+        if (hit) {
+            rec.S[0] = f4(S1, 0.f); rec.S[1] = f4(S2, 0.f); rec.S[2] = f4(S3, 0.f); rec.S[3] = f4(S4, 0.f);
+            rec.ia = (uint32_t)a1 | ((uint32_t)a2 << 8) | ((uint32_t)a3 << 16) | ((uint32_t)a4 << 24);
+            rec.ib = (uint32_t)b1 | ((uint32_t)b2 << 8) | ((uint32_t)b3 << 16) | ((uint32_t)b4 << 24);
+            return 1;
+        }
+        f3 n1, n2, n3;
+        int na1, nb1, na2, nb2, na3, nb3;
+        if (todel == 1) { n1 = S2; na1 = a2; nb1 = b2; n2 = S3; na2 = a3; nb2 = b3; n3 = S4; na3 = a4; nb3 = b4; }
+        else if (todel == 2) { n1 = S3; na1 = a3; nb1 = b3; n2 = S1; na2 = a1; nb2 = b1; n3 = S4; na3 = a4; nb3 = b4; }
+        else { n1 = S1; na1 = a1; nb1 = b1; n2 = S2; na2 = a2; nb2 = b2; n3 = S4; na3 = a4; nb3 = b4; }
+        S1 = n1; a1 = na1; b1 = nb1; S2 = n2; a2 = na2; b2 = nb2; S3 = n3; a3 = na3; b3 = nb3;
+    }
+    return -1;
+}
+
+template <int LPP>
+__global__ void __launch_bounds__(NARROW_THREADS, 6) gjk_pass_kernel(NarrowArgs a)
+{
+    constexpr int GPB = NARROW_THREADS / LPP;
+    const int grp = threadIdx.x / LPP;
+    Group<LPP> g;
+    g.lane = threadIdx.x % LPP;
+    g.mask = LPP == 32 ? 0xffffffffu : (((1u << LPP) - 1u) << ((threadIdx.x & 31) / LPP * LPP));
+    const int64_t m = *a.n_pairs_dev;
+    const int64_t n = m < a.pair_cap ? m : a.pair_cap;
+    const double4* pos = reinterpret_cast<const double4*>(a.st.pos);
+    const int2* pairs = reinterpret_cast<const int2*>(a.pairs);
+    const float4* wv = reinterpret_cast<const float4*>(a.st.world_verts);
+    SimplexRec* recs = reinterpret_cast<SimplexRec*>(a.epa_rec);
+    const int64_t stride = (int64_t)gridDim.x * GPB * LPP;
+    for (int64_t base = ((int64_t)blockIdx.x * GPB + grp) * LPP; base < n; base += stride) {
+        // sphere pre-test, one candidate per lane (see narrow_kernel)
+        const int64_t Pl = base + g.lane;
+        bool live = false;
+        if (Pl < n) {
+            const int2 pr = pairs[Pl];
+            const double4 pa = pos[pr.x], pb = pos[pr.y];
+            const float dx = (float)(pb.x - pa.x), dy = (float)(pb.y - pa.y), dz = (float)(pb.z - pa.z);
+            const float mag = fmaxf(fmaxf(fabsf((float)pa.x), fabsf((float)pa.y)), fabsf((float)pa.z)) +
+                              fmaxf(fmaxf(fabsf((float)pb.x), fabsf((float)pb.y)), fabsf((float)pb.z));
+            const float r = (float)(pa.w + pb.w) * 1.001f + 1e-5f * mag + 1e-6f;
+            live = dx * dx + dy * dy + dz * dz <= r * r;
+            if (!live && a.collision) a.collision[Pl] = 0;
+        }
+        unsigned msk = g.ballot(live);
+        while (msk) {
+            const int l = __ffs(msk) - 1;
+            msk &= msk - 1;
+            const int64_t P = base + l;
+            const int2 pr = pairs[P];
+            const double4 pa = pos[pr.x], pb = pos[pr.y];
+            const f3 cA = mk3((float)pa.x, (float)pa.y, (float)pa.z);
+            const f3 cB = mk3((float)pb.x, (float)pb.y, (float)pb.z);
+            const int oa = a.st.vert_off[pr.x], ob = a.st.vert_off[pr.y];
+            const int nA = a.st.vert_off[pr.x + 1] - oa, nB = a.st.vert_off[pr.y + 1] - ob;
+            Work3 wk = {0u, 0u, 0u};
+            SimplexRec rec;
+            int out = 0;
+            const bool ok = nA <= a.hull_cap && nB <= a.hull_cap;
+            if (ok) out = gjk_decide<LPP>(g, wv + oa, nA, wv + ob, nB, cA, cB, rec, wk);
+            if (g.lane == 0) {
+                if (!ok) {
+                    set_status(a.status, MWD_ST_BAD_SHAPE);
+                    if (a.collision) a.collision[P] = -1;
+                } else if (out == 1) {
+                    const int slot = atomicAdd(a.epa_count, 1);
+                    if (slot < a.epa_cap) {
+                        rec.P = P;
+                        recs[slot] = rec;
+                    } else {
+                        set_status(a.status, MWD_ST_PAIR_OVERFLOW);
+                    }
+                    if (a.collision) a.collision[P] = 1;
+                } else {
+                    // undecided pairs add zero force in the reference (.cu:1304-1319): nothing to add
+                    if (out == -1) set_status(a.status, MWD_ST_GJK_NOCONV);
+                    if (a.collision) a.collision[P] = out;
+                }
+                if (a.work_counters) {
+                    atomicAdd(a.work_counters + 0, (unsigned long long)wk.dots);
+                    atomicAdd(a.work_counters + 2, (unsigned long long)wk.queries);
+                }
+            }
+            g.sync();
+        }
+    }
+}
+
+template <int LPP>
+__global__ void __launch_bounds__(NARROW_THREADS) epa_pass_kernel(NarrowArgs a)
+{
+    extern __shared__ float4 smem[];
+    constexpr int GPB = NARROW_THREADS / LPP;
+    const int grp = threadIdx.x / LPP;
+    Group<LPP> g;
+    g.lane = threadIdx.x % LPP;
+    g.mask = LPP == 32 ? 0xffffffffu : (((1u << LPP) - 1u) << ((threadIdx.x & 31) / LPP * LPP));
+    EpaMem* em = reinterpret_cast<EpaMem*>(smem) + grp;
+    float4* hull = reinterpret_cast<float4*>(reinterpret_cast<EpaMem*>(smem) + GPB) + (size_t)grp * 2 * a.hull_cap;
+    float4* hA = hull;
+    float4* hB = hull + a.hull_cap;
+    const int cnt = *a.epa_count;
+    const int64_t m = cnt < a.epa_cap ? cnt : a.epa_cap;
+    const SimplexRec* recs = reinterpret_cast<const SimplexRec*>(a.epa_rec);
+    for (int64_t i = (int64_t)blockIdx.x * GPB + grp; i < m; i += (int64_t)gridDim.x * GPB) {
+        const SimplexRec rec = recs[i];
+        const int64_t P = rec.P;
+        PairView p;
+        load_pair<1>(a, P, p, hA, hB, g.lane, LPP);
+        g.sync();
+        const mwd_material& M = a.scenes[a.st.info[p.idA] >> 1].mat[p.wall];
+        Work3 wk = {0u, 0u, 0u};
+        f3 S1 = xyz(rec.S[0]), S2 = xyz(rec.S[1]), S3 = xyz(rec.S[2]), S4 = xyz(rec.S[3]);
+        int a1 = rec.ia & 0xff, a2 = (rec.ia >> 8) & 0xff, a3 = (rec.ia >> 16) & 0xff, a4 = rec.ia >> 24;
+        int b1 = rec.ib & 0xff, b2 = (rec.ib >> 8) & 0xff, b3 = (rec.ib >> 16) & 0xff, b4 = rec.ib >> 24;
+        if (is_flat(S1, S2, S3, S4)) {
+            f3 d4 = cross(S1, S2);
+            support<LPP>(g, hA, p.nA, hB, p.nB, d4, S4, a4, b4, wk);
+        }
+        EpaResult er;
+        epa<LPP>(g, *em, hA, p.nA, hB, p.nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er, wk);
+        ForceResult fo;
+        contact_force(p.cA, p.cB, er.depth, er.n, er.cpA, er.cpB, M, p.vA, p.vB, p.wA, p.wB, p.dt, p.qA, p.dtn, p.IsA,
+                      p.IsB, fo);
+        if (g.lane == 0) {
+            set_status(a.status, er.status);
+            accumulate<1>(a, p, fo);
+            if (a.face_ids) {
+                int* fid = a.face_ids + 6 * P;
+                for (int k = 0; k < 3; ++k) {
+                    fid[k] = er.fa[k];
+                    fid[3 + k] = er.fb[k];
+                }
+            }
+            if (a.work_counters) {
+                atomicAdd(a.work_counters + 0, (unsigned long long)wk.dots);
+                atomicAdd(a.work_counters + 1, (unsigned long long)wk.faces);
+                atomicAdd(a.work_counters + 2, (unsigned long long)wk.queries);
+            }
+        }
+        g.sync();
+    }
+}
+
+template <int LPP>
+int launch_two_pass_lpp(const NarrowArgs& a, cudaStream_t s)
+{
+    constexpr int GPB = NARROW_THREADS / LPP;
+    // occupancy queried once per (kernel, shared-memory size); no runtime calls during capture after that
+    static int gjk_per_sm = 0;
+    static size_t epa_shm_cached = 0;
+    static int epa_per_sm = 0;
+    static bool attr = false;
+    if (!gjk_per_sm) {
+        int v = 0;
+        MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, gjk_pass_kernel<LPP>, NARROW_THREADS, 0));
+        gjk_per_sm = v < 1 ? 1 : v;
+    }
+    const size_t shm = (size_t)GPB * sizeof(EpaMem) + (size_t)GPB * 2 * a.hull_cap * sizeof(float4);
+    if (!attr) {
+        MWD_CUDA(cudaFuncSetAttribute(epa_pass_kernel<LPP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        attr = true;
+    }
+    if (shm != epa_shm_cached || !epa_per_sm) {
+        int v = 0;
+        MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, epa_pass_kernel<LPP>, NARROW_THREADS, shm));
+        epa_per_sm = v < 1 ? 1 : v;
+        epa_shm_cached = shm;
+    }
+    MWD_CUDA(cudaMemsetAsync(a.epa_count, 0, sizeof(int32_t), s));
+    gjk_pass_kernel<LPP><<<(unsigned)(num_sms() * gjk_per_sm), NARROW_THREADS, 0, s>>>(a);
+    epa_pass_kernel<LPP><<<(unsigned)(num_sms() * epa_per_sm), NARROW_THREADS, shm, s>>>(a);
+    MWD_CUDA(cudaGetLastError());
+    return MWD_OK;
+}
+
 // Resolve the reference's overlapping stride-1 history writes (.cu:1018-1021, :1158-1161): the
 // value left at hist[k] is the one written by the highest pair index P' in [k-3, k] that wrote.
 __global__ void hist_resolve_kernel(float* hist, const float4* stage, const uint8_t* wrote, int64_t n)
@@ -763,6 +986,18 @@ int launch_narrow(const NarrowArgs& a, int mode, int lanes, int64_t n_hint, cuda
             case 16: return launch_lpp<16, 1>(a, n_hint, s);
             case 32: return launch_lpp<32, 1>(a, n_hint, s);
         }
+    }
+    set_error("lanes per pair must be 4, 8, 16 or 32 (got %d)", lanes);
+    return MWD_ERR_INVALID;
+}
+
+int launch_narrow_two_pass(const NarrowArgs& a, int lanes, cudaStream_t s)
+{
+    switch (lanes) {
+        case 4: return launch_two_pass_lpp<4>(a, s);
+        case 8: return launch_two_pass_lpp<8>(a, s);
+        case 16: return launch_two_pass_lpp<16>(a, s);
+        case 32: return launch_two_pass_lpp<32>(a, s);
     }
     set_error("lanes per pair must be 4, 8, 16 or 32 (got %d)", lanes);
     return MWD_ERR_INVALID;

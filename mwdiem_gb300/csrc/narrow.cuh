@@ -37,9 +37,14 @@ struct NarrowArgs {
     unsigned long long* work_counters;  // optional (3,): vertex dot products, EPA faces, support queries
     int32_t hull_cap;       // hull vertices staged per side
     int32_t pad1;
+    // two-pass mode (table mode): list of pairs in contact and the simplex GJK stopped on
+    int32_t* epa_count;
+    void* epa_rec;          // (epa_cap,) 80-byte records
+    int64_t epa_cap;
 };
 
 int launch_narrow(const NarrowArgs& a, int mode, int lanes, int64_t n_hint, cudaStream_t s);
+int launch_narrow_two_pass(const NarrowArgs& a, int lanes, cudaStream_t s);
 int launch_hist_resolve(float* hist, const float* stage, const uint8_t* wrote, int64_t n, cudaStream_t s);
 size_t narrow_smem_bytes(int lpp, int hull_cap);
 

@@ -36,7 +36,7 @@ class Layout:
 
 
 class Simulator:
-    def __init__(self, scenes, lanes=8, pair_cap=None, device="cuda", collect_collisions=False):
+    def __init__(self, scenes, lanes=8, pair_cap=None, device="cuda", collect_collisions=False, two_pass=True):
         _dev.require_cuda()
         if isinstance(scenes, SceneSpec):
             scenes = [scenes]
@@ -45,6 +45,7 @@ class Simulator:
         self.device = torch.device(device)
         self._build_state()
         self._build_scenes()
+        self.two_pass = bool(two_pass)
         self._build_work(pair_cap, collect_collisions)
         self.graph = None
         self.graph_steps = 0
@@ -205,6 +206,12 @@ class Simulator:
         wk.crowded_cap = crowded_cap
         w["work_counters"] = torch.zeros(3, dtype=torch.int64, device=self.device)
         wk.work_counters = None
+        if self.two_pass:
+            w["epa_count"] = torch.zeros(1, **i32)
+            w["epa_rec"] = torch.zeros(cap * 80, dtype=torch.uint8, device=self.device)
+            wk.epa_count = w["epa_count"].data_ptr()
+            wk.epa_rec = w["epa_rec"].data_ptr()
+            wk.epa_cap = cap
         wk.total_cells = self.total_cells
         wk.pair_cap = cap
         self.work = wk

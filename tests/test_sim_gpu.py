@@ -123,3 +123,25 @@ def test_batched_equals_separate():
         rows = batch.particle_rows(i)
         d = np.abs(batch.positions()[rows].cpu().numpy() - one.positions(0).cpu().numpy()).max()
         assert d <= 1e-6 * 16.0
+
+
+def test_two_pass_equals_single_pass():
+    # the GJK pass + EPA pass split must not change any decision: same flags, same forces up to the
+    # float-atomic summation order
+    from mwdiem_gb300.sim import Simulator
+    sp = dense_scene(n=800, seed=11)
+    one = Simulator(sp, collect_collisions=True, two_pass=False)
+    two = Simulator(sp, collect_collisions=True, two_pass=True)
+    for s in (one, two):
+        s.broadphase()
+        s.narrow_force()
+    torch.cuda.synchronize()
+    n = one.n_pairs()
+    assert n == two.n_pairs()
+    c1 = one.w["collision"][:n].cpu().numpy()
+    c2 = two.w["collision"][:n].cpu().numpy()
+    assert np.array_equal(c1, c2) and (c1 == 1).sum() > 100
+    F1, F2 = one.t["force"].cpu().numpy(), two.t["force"].cpu().numpy()
+    assert np.abs(F1 - F2).max() <= 1e-5 * np.abs(F1).max()
+    T1, T2 = one.t["torque"].cpu().numpy(), two.t["torque"].cpu().numpy()
+    assert np.abs(T1 - T2).max() <= 1e-5 * np.abs(T1).max()
