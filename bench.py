@@ -35,7 +35,7 @@ WORKLOAD = ("pour20k: 20,000 convex hulls of U{12..32} points on a sphere of rad
             "lattice (spacing 2.6) in a 40x40 box, random orientations, at rest, gravity; kn 1e5, damping "
             "ratio 0.3 (en=et=0.372), mu 0.5, dt 5e-5")
 METRIC = "particle-steps/s"
-KERNELS_PER_STEP = 14  # broad phase 12 (assign, 3 scan, scatter, order, crowded, count, 3 scan, emit) + narrow + integrate
+KERNELS_PER_STEP = 13  # broad phase 10 (assign, 2 scan, scatter, order, crowded, count, 2 scan, emit) + GJK pass + EPA pass + integrate
 
 
 def parse():

@@ -68,30 +68,16 @@ __global__ void scan_reduce_kernel(const int32_t* in, int64_t n, int32_t* block_
     if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
 }
 
-__global__ void scan_blocks_kernel(int32_t* block_sums, int nb)
-{
-    __shared__ int sh[SCAN_THREADS / 32];
-    __shared__ int carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (int base = 0; base < nb; base += SCAN_THREADS) {
-        int i = base + threadIdx.x;
-        int v = i < nb ? block_sums[i] : 0;
-        int tot;
-        int ex = block_exclusive_scan(v, sh, &tot);
-        if (i < nb) block_sums[i] = ex + carry;
-        __syncthreads();
-        if (threadIdx.x == 0) carry += tot;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) block_sums[nb] = carry;
-}
-
-// out[i] = sum(in[0..i)), out[n] = total; in and out may alias
+// out[i] = sum(in[0..i)), out[n] = total; in and out may alias.  Each block adds up the tile totals
+// of the blocks before it (at most a few thousand values), so no separate pass scans the totals.
 __global__ void scan_final_kernel(const int32_t* in, int64_t n, const int32_t* block_sums, int32_t* out, int nb,
                                   int64_t* total_out, int64_t cap, uint32_t* status, uint32_t overflow_bit)
 {
     __shared__ int sh[SCAN_THREADS / 32];
+    int part = 0;
+    for (int i = threadIdx.x; i < (int)blockIdx.x; i += SCAN_THREADS) part += block_sums[i];
+    int offset;
+    block_exclusive_scan(part, sh, &offset);  // offset = sum over the whole block
     int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
     int v[SCAN_ITEMS];
     int s = 0;
@@ -101,14 +87,14 @@ __global__ void scan_final_kernel(const int32_t* in, int64_t n, const int32_t* b
         s += v[k];
     }
     int tot;
-    int ex = block_exclusive_scan(s, sh, &tot) + block_sums[blockIdx.x];
+    int ex = block_exclusive_scan(s, sh, &tot) + offset;
     for (int k = 0; k < SCAN_ITEMS; ++k) {
         int64_t i = base + k;
         if (i < n) out[i] = ex;
         ex += v[k];
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        int64_t t = block_sums[nb];
+    if ((int)blockIdx.x == nb - 1 && threadIdx.x == 0) {
+        int64_t t = (int64_t)offset + tot;
         out[n] = (int32_t)t;
         if (total_out) *total_out = t < cap ? t : cap;
         if (t > cap) set_status(status, overflow_bit);
@@ -338,7 +324,11 @@ __global__ void pairs_kernel(BroadArgs a)
     int32_t* pairs = a.pairs;
     const int64_t cap = a.pair_cap;
     if (EMIT) out = a.pair_count[t];
+    const double4* P4 = reinterpret_cast<const double4*>(a.pos);
+    const double4 pr4 = a.cull ? P4[r] : make_double4(0, 0, 0, 0);
     auto put = [&](int A, int B) {
+        // optional exact-outcome filter: pairs the reference's GJK rejects at its first test
+        if (a.cull && spheres_apart(pr4, P4[B])) return;
         if (EMIT) {
             if (out < cap) reinterpret_cast<int2*>(pairs)[out] = make_int2(A, B);
             ++out;
@@ -446,7 +436,6 @@ int launch_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* tmp, int64_
     const int nb = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
     const int nbl = nb > 0 ? nb : 1;
     scan_reduce_kernel<<<nbl, SCAN_THREADS, 0, s>>>(in, n, tmp);
-    scan_blocks_kernel<<<1, SCAN_THREADS, 0, s>>>(tmp, nbl);
     scan_final_kernel<<<nbl, SCAN_THREADS, 0, s>>>(in, n, tmp, out, nbl, total_out, cap, status, overflow_bit);
     MWD_CUDA(cudaGetLastError());
     return MWD_OK;

@@ -13,7 +13,7 @@ struct BroadArgs {
     const int32_t* info;         // (n,) scene << 1 | is_wall, or NULL: one scene, no walls
     const mwd_scene* scenes;     // device scene table
     int32_t walls;               // 1: emit wall candidates
-    int32_t pad;
+    int32_t cull;                // 1: drop pairs whose bounding spheres are apart (pos.w = radius)
     int32_t* cell_count;         // (total_cells,) zero on entry and on exit
     int32_t* cell_start;         // (total_cells+1,)
     int32_t* cell_of;            // (n,)

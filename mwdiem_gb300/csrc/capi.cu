@@ -394,6 +394,7 @@ int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_s
     a.status = work->status;
     a.total_cells = work->total_cells;
     a.pair_cap = work->pair_cap;
+    a.cull = work->cull_pairs ? 1 : 0;
     return launch_broad(a, reinterpret_cast<cudaStream_t>(stream));
 }
 
@@ -425,6 +426,7 @@ int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work*
         a.epa_count = work->epa_count;
         a.epa_rec = work->epa_rec;
         a.epa_cap = work->epa_cap;
+        a.pre_culled = work->cull_pairs ? 1 : 0;
         return launch_narrow_two_pass(a, lp, reinterpret_cast<cudaStream_t>(stream));
     }
     return launch_narrow(a, 1, lp, -1, reinterpret_cast<cudaStream_t>(stream));

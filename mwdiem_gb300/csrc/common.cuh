@@ -56,6 +56,21 @@ __host__ __device__ __forceinline__ f3 qtrip(float4 q1, f3 v, float4 q2)
     return mk3(m2.y, m2.z, m2.w);
 }
 
+// Bounding-sphere test of two rows (pos.xyz = centre, pos.w = largest vertex distance from it).
+// True when the centres are farther apart than rA + rB plus a rounding margin.  For such a pair the
+// reference's first GJK test, d.(a* - b*) < 0 with d = cB - cA (gpu_fine_contact_detection.cu:1010-1023),
+// is negative: d.a* <= d.cA + |d| rA and -d.b* <= -d.cB + |d| rB give d.(a* - b*) <= -|d| (|d| - rA - rB).
+// The margin (1e-3 relative, 1e-5 of the coordinate magnitude) covers the FP32 rounding of the
+// centres, the world vertices and the dot product, so the reference classifies the pair "no contact".
+__device__ __forceinline__ bool spheres_apart(double4 pa, double4 pb)
+{
+    const float dx = (float)(pb.x - pa.x), dy = (float)(pb.y - pa.y), dz = (float)(pb.z - pa.z);
+    const float mag = fmaxf(fmaxf(fabsf((float)pa.x), fabsf((float)pa.y)), fabsf((float)pa.z)) +
+                      fmaxf(fmaxf(fabsf((float)pb.x), fabsf((float)pb.y)), fabsf((float)pb.z));
+    const float r = (float)(pa.w + pb.w) * 1.001f + 1e-5f * mag + 1e-6f;
+    return dx * dx + dy * dy + dz * dz > r * r;
+}
+
 __device__ __forceinline__ void set_status(uint32_t* st, uint32_t bits)
 {
     if (st && bits) atomicOr(st, bits);

@@ -318,20 +318,31 @@ __global__ void __launch_bounds__(RB) integrate_kernel(mwd_state st, const mwd_s
     const int v0 = s_off[0], v1 = s_off[rows];
     const float4* bv = reinterpret_cast<const float4*>(st.body_verts);
     float4* wv = reinterpret_cast<float4*>(st.world_verts);
-    for (int j = v0 + threadIdx.x; j < v1; j += RB) {
-        // owner row: last r with s_off[r] <= j
-        int lo = 0, hi = rows - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (s_off[mid] <= j) lo = mid; else hi = mid - 1;
+    constexpr int U = 4;  // vertices in flight per thread: loads first, then the stores
+    for (int j0 = v0 + threadIdx.x; j0 < v1; j0 += U * RB) {
+        float4 r0[U];
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+            const int j = j0 + k * RB;
+            r0[k] = j < v1 ? __ldg(bv + j) : make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        const float* R = s_R[lo];
-        const float* c = s_c[lo];
-        float4 r0 = bv[j];
-        float rx = R[0] * r0.x + R[1] * r0.y + R[2] * r0.z;
-        float ry = R[3] * r0.x + R[4] * r0.y + R[5] * r0.z;
-        float rz = R[6] * r0.x + R[7] * r0.y + R[8] * r0.z;
-        wv[j] = make_float4(c[0] + (rx + c[1]), c[2] + (ry + c[3]), c[4] + (rz + c[5]), 0.f);
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+            const int j = j0 + k * RB;
+            if (j >= v1) break;
+            // owner row: last r with s_off[r] <= j
+            int lo = 0, hi = rows - 1;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (s_off[mid] <= j) lo = mid; else hi = mid - 1;
+            }
+            const float* R = s_R[lo];
+            const float* c = s_c[lo];
+            float rx = R[0] * r0[k].x + R[1] * r0[k].y + R[2] * r0[k].z;
+            float ry = R[3] * r0[k].x + R[4] * r0[k].y + R[5] * r0[k].z;
+            float rz = R[6] * r0[k].x + R[7] * r0[k].y + R[8] * r0[k].z;
+            wv[j] = make_float4(c[0] + (rx + c[1]), c[2] + (ry + c[3]), c[4] + (rz + c[5]), 0.f);
+        }
     }
 }
 

@@ -656,12 +656,8 @@ __global__ void __launch_bounds__(NARROW_THREADS) narrow_kernel(NarrowArgs a)
         n = m < a.pair_cap ? m : a.pair_cap;
     }
     if (MODE == 1) {
-        // Sphere pre-test, LPP candidate pairs at a time (one per lane).  pos.w holds each row's
-        // bounding radius (largest vertex distance from the centre).  When the centres are farther
-        // apart than rA + rB plus a rounding margin, the reference's first GJK test,
-        // d.(a* - b*) < 0 with d = cB - cA (gpu_fine_contact_detection.cu:1010-1023), is negative:
-        // d.a* <= d.cA + |d| rA and -d.b* <= -d.cB + |d| rB give d.(a* - b*) <= -|d| (|d| - rA - rB).
-        // Such pairs get the reference's outcome (collision 0, no force) without running GJK.
+        // sphere pre-test (spheres_apart), LPP candidate pairs at a time (one per lane); pairs it
+        // settles get the reference's outcome (collision 0, no force) without running GJK
         const double4* pos = reinterpret_cast<const double4*>(a.st.pos);
         const int2* pairs = reinterpret_cast<const int2*>(a.pairs);
         const int64_t stride = (int64_t)gridDim.x * GPB * LPP;
@@ -670,12 +666,7 @@ __global__ void __launch_bounds__(NARROW_THREADS) narrow_kernel(NarrowArgs a)
             bool live = false;
             if (Pl < n) {
                 const int2 pr = pairs[Pl];
-                const double4 pa = pos[pr.x], pb = pos[pr.y];
-                const float dx = (float)(pb.x - pa.x), dy = (float)(pb.y - pa.y), dz = (float)(pb.z - pa.z);
-                const float mag = fmaxf(fmaxf(fabsf((float)pa.x), fabsf((float)pa.y)), fabsf((float)pa.z)) +
-                                  fmaxf(fmaxf(fabsf((float)pb.x), fabsf((float)pb.y)), fabsf((float)pb.z));
-                const float r = (float)(pa.w + pb.w) * 1.001f + 1e-5f * mag + 1e-6f;
-                live = dx * dx + dy * dy + dz * dz <= r * r;
+                live = !spheres_apart(pos[pr.x], pos[pr.y]);
                 if (!live && a.collision) a.collision[Pl] = 0;
             }
             unsigned m = g.ballot(live);
@@ -770,22 +761,25 @@ __global__ void __launch_bounds__(NARROW_THREADS, 6) gjk_pass_kernel(NarrowArgs 
     const int2* pairs = reinterpret_cast<const int2*>(a.pairs);
     const float4* wv = reinterpret_cast<const float4*>(a.st.world_verts);
     SimplexRec* recs = reinterpret_cast<SimplexRec*>(a.epa_rec);
-    const int64_t stride = (int64_t)gridDim.x * GPB * LPP;
-    for (int64_t base = ((int64_t)blockIdx.x * GPB + grp) * LPP; base < n; base += stride) {
-        // sphere pre-test, one candidate per lane (see narrow_kernel)
-        const int64_t Pl = base + g.lane;
-        bool live = false;
-        if (Pl < n) {
-            const int2 pr = pairs[Pl];
-            const double4 pa = pos[pr.x], pb = pos[pr.y];
-            const float dx = (float)(pb.x - pa.x), dy = (float)(pb.y - pa.y), dz = (float)(pb.z - pa.z);
-            const float mag = fmaxf(fmaxf(fabsf((float)pa.x), fabsf((float)pa.y)), fabsf((float)pa.z)) +
-                              fmaxf(fmaxf(fabsf((float)pb.x), fabsf((float)pb.y)), fabsf((float)pb.z));
-            const float r = (float)(pa.w + pb.w) * 1.001f + 1e-5f * mag + 1e-6f;
-            live = dx * dx + dy * dy + dz * dz <= r * r;
-            if (!live && a.collision) a.collision[Pl] = 0;
+    // pre_culled: the broad phase already dropped the pairs whose spheres are apart, so every listed
+    // pair needs GJK and each group takes one pair at a time; otherwise LPP candidates are
+    // sphere-tested at once (one per lane) and the survivors run GJK
+    const int chunk = a.pre_culled ? 1 : LPP;
+    const int64_t stride = (int64_t)gridDim.x * GPB * chunk;
+    for (int64_t base = ((int64_t)blockIdx.x * GPB + grp) * chunk; base < n; base += stride) {
+        unsigned msk;
+        if (a.pre_culled) {
+            msk = 1u;
+        } else {
+            const int64_t Pl = base + g.lane;
+            bool live = false;
+            if (Pl < n) {
+                const int2 pr = pairs[Pl];
+                live = !spheres_apart(pos[pr.x], pos[pr.y]);
+                if (!live && a.collision) a.collision[Pl] = 0;
+            }
+            msk = g.ballot(live);
         }
-        unsigned msk = g.ballot(live);
         while (msk) {
             const int l = __ffs(msk) - 1;
             msk &= msk - 1;

@@ -41,6 +41,8 @@ struct NarrowArgs {
     int32_t* epa_count;
     void* epa_rec;          // (epa_cap,) 80-byte records
     int64_t epa_cap;
+    int32_t pre_culled;     // the pair list holds only pairs whose bounding spheres overlap
+    int32_t pad2;
 };
 
 int launch_narrow(const NarrowArgs& a, int mode, int lanes, int64_t n_hint, cudaStream_t s);

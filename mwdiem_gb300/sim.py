@@ -36,7 +36,8 @@ class Layout:
 
 
 class Simulator:
-    def __init__(self, scenes, lanes=8, pair_cap=None, device="cuda", collect_collisions=False, two_pass=True):
+    def __init__(self, scenes, lanes=8, pair_cap=None, device="cuda", collect_collisions=False, two_pass=True,
+                 cull_pairs=True):
         _dev.require_cuda()
         if isinstance(scenes, SceneSpec):
             scenes = [scenes]
@@ -46,6 +47,7 @@ class Simulator:
         self._build_state()
         self._build_scenes()
         self.two_pass = bool(two_pass)
+        self.cull_pairs = bool(cull_pairs)
         self._build_work(pair_cap, collect_collisions)
         self.graph = None
         self.graph_steps = 0
@@ -212,6 +214,7 @@ class Simulator:
             wk.epa_count = w["epa_count"].data_ptr()
             wk.epa_rec = w["epa_rec"].data_ptr()
             wk.epa_cap = cap
+        wk.cull_pairs = 1 if self.cull_pairs else 0
         wk.total_cells = self.total_cells
         wk.pair_cap = cap
         self.work = wk

@@ -34,7 +34,7 @@ def oriented(p):
 def test_pairs_flags_forces_step0():
     from mwdiem_gb300.sim import Simulator
     sp = dense_scene()
-    sim = Simulator(sp, collect_collisions=True)
+    sim = Simulator(sp, collect_collisions=True, cull_pairs=False)
     ref = stepper.RefStepper(sp)
     sim.broadphase()
     pairs = sim.pairs().cpu().numpy()
@@ -145,3 +145,28 @@ def test_two_pass_equals_single_pass():
     assert np.abs(F1 - F2).max() <= 1e-5 * np.abs(F1).max()
     T1, T2 = one.t["torque"].cpu().numpy(), two.t["torque"].cpu().numpy()
     assert np.abs(T1 - T2).max() <= 1e-5 * np.abs(T1).max()
+
+
+def test_sphere_filter_drops_only_noncontacts():
+    # with cull_pairs the broad phase lists a subset of the reference's candidates; every dropped
+    # candidate must be one the FP32 oracle, fed the GPU's own vertices, classifies "no contact"
+    from mwdiem_gb300.sim import Simulator
+    sp = dense_scene(n=700, seed=12)
+    full = Simulator(sp, collect_collisions=True, cull_pairs=False)
+    cut = Simulator(sp, collect_collisions=True, cull_pairs=True)
+    full.broadphase()
+    cut.broadphase()
+    pf = full.pairs().cpu().numpy()
+    pc = cut.pairs().cpu().numpy()
+    kept = oriented(pc)
+    assert kept <= oriented(pf) and len(kept) < len(pf)
+    ref = stepper.RefStepper(sp)
+    o = oracle.contact(stepper.gather_from_sim(full, pf, ref.V), ref.params, full.n, "f32", face_cap=128)
+    dropped = np.array([tuple(p) not in kept for p in pf.tolist()])
+    assert np.all(o["collision"][dropped] == 0)
+    assert np.all(o["counters"][dropped, 0] == 1)   # settled by the first support query
+    cut.narrow_force()
+    full.narrow_force()
+    torch.cuda.synchronize()
+    F1, F2 = full.t["force"].cpu().numpy(), cut.t["force"].cpu().numpy()
+    assert np.abs(F1 - F2).max() <= 1e-5 * np.abs(F1).max()
