@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-breakdown", action="store_true")
+    ap.add_argument("--pairs", type=int, default=1 << 22,
+                    help="also time the narrow phase on this many independent random pairs (0: skip)")
     return ap.parse_args()
 
 
@@ -234,6 +236,10 @@ def main():
 
     if rank == 0 and not args.no_breakdown:
         line["breakdown"], line["roofline"] = breakdown(sim, V, flush)
+    if rank == 0 and args.pairs > 0:
+        del sim
+        torch.cuda.empty_cache()
+        line["narrow_pairs"] = pairs_rate(args.pairs, args.lanes)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
             cb, _ = cpu_path_rate(build_scene(SCENE["seed"]))
@@ -301,6 +307,42 @@ def breakdown(sim, V, flush, reps=10):
                 "frac": a / hbm, "traffic": None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in pk else "fallback 6800"}
     return out, roof
+
+
+def pairs_rate(n_pairs, lanes, reps=5):
+    """GJK/EPA pairs/s of the device-step narrow phase on independent random pairs (hulls of 8-64
+    vertices, radius U[0.8,1.2], centre distance U[0.5,2.2] (rA+rB)/2; inputs ~10 GB, far above L2)."""
+    import ctypes as C
+
+    import torch
+    from mwdiem_gb300 import _lib
+    from mwdiem_gb300.pairbench import PairScene
+    ps = PairScene(n_pairs, seed=1, lanes=lanes)
+    ps.narrow()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        ps.narrow()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    ps.narrow(count_work=True)
+    torch.cuda.synchronize()
+    dots, faces, queries = (int(x) for x in ps.w["counters"].cpu().numpy())
+    coll = ps.w["collision"].cpu().numpy()
+    flops = 5.0 * dots + 60.0 * faces
+    scratch = torch.zeros(8 * 1024, dtype=torch.float32, device="cuda")
+    tf = C.c_double(0)
+    _lib.check(_lib.lib().mwd_probe_fp32(20000, scratch.data_ptr(), C.byref(tf), None))
+    ach = flops / (ms * 1e-3) / 1e12
+    return {"pairs": n_pairs, "ms_per_launch": ms, "pairs_per_s": n_pairs / (ms * 1e-3),
+            "contact_fraction": float((coll == 1).mean()), "support_queries": queries, "vertex_dots": dots,
+            "epa_faces": faces, "lanes_per_pair": lanes, "two_pass": True,
+            "roofline": {"kernel": "gjk_pass + epa_pass", "bound": "fp32", "achieved": ach, "peak": tf.value,
+                         "unit": "TFLOP/s", "frac": ach / tf.value if tf.value else None,
+                         "peak_source": "measured in this run (mwd_probe_fp32)"}}
 
 
 def reference_arm(args):

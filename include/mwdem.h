@@ -243,6 +243,8 @@ typedef struct {
     int32_t* epa_count;    /* (1,) two-pass narrow phase: pairs found in contact by the GJK pass */
     void* epa_rec;         /* (epa_cap, 80 B): their simplex; NULL selects the single-pass kernel */
     int64_t epa_cap;
+    float* sorted_pos;     /* (n,4) centre and radius of each row in cell order (used with cull_pairs) */
+    int32_t* sorted_cell;  /* (n,) cell of each row in cell order (used with cull_pairs) */
     int32_t cull_pairs;    /* 1: the broad phase lists only pairs whose bounding spheres (pos.w) overlap
                               within a rounding margin -- the others are exactly the candidates the
                               reference's first GJK test rejects; 0: the reference's full candidate list */

@@ -230,6 +230,17 @@ __global__ void scatter_kernel(BroadArgs a)
     a.scatter_out[a.cell_start[g] + slot] = r;
 }
 
+// write row v at sorted position i of cell g, with its centre/radius and cell alongside
+__device__ __forceinline__ void place(const BroadArgs& a, int i, int v, int g)
+{
+    a.sorted[i] = v;
+    if (a.sorted_pos) {
+        const double4 p = reinterpret_cast<const double4*>(a.pos)[v];
+        a.sorted_pos[i] = make_float4((float)p.x, (float)p.y, (float)p.z, (float)p.w);
+        a.sorted_cell[i] = g;
+    }
+}
+
 __global__ void order_kernel(BroadArgs a)
 {
     const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
@@ -239,7 +250,7 @@ __global__ void order_kernel(BroadArgs a)
     const int s = a.cell_start[g], e = a.cell_start[g + 1];
     const int k = e - s;
     if (k == 1) {
-        a.sorted[s] = r;
+        place(a, s, r, g);
         return;
     }
     for (int j = s; j < e; ++j)
@@ -265,7 +276,7 @@ __global__ void order_kernel(BroadArgs a)
     unsigned char used[SMALL_TAB], used2[SMALL_TAB];
     const int base = a.info ? a.scenes[scene_of(a, r)].row_begin : 0;
     pyset_order<SMALL_TAB>(m, k, o, tab, used, tmp, used2, base);
-    for (int j = 0; j < k; ++j) a.sorted[s + j] = o[j];
+    for (int j = 0; j < k; ++j) place(a, s + j, o[j], g);
 }
 
 // one warp per crowded cell: members ranked by id in parallel, then lane 0 replays the set inserts
@@ -286,7 +297,7 @@ __global__ void __launch_bounds__(32) order_crowded_kernel(BroadArgs a)
             for (int j = threadIdx.x; j < k; j += 32) {
                 int v = a.scatter_out[s + j], rank = 0;
                 for (int i = 0; i < k; ++i) rank += a.scatter_out[s + i] < v;
-                a.sorted[s + rank] = v;
+                place(a, s + rank, v, g);
             }
             if (threadIdx.x == 0) set_status(a.status, MWD_ST_CELL_CROWDED);
             __syncwarp();
@@ -301,7 +312,7 @@ __global__ void __launch_bounds__(32) order_crowded_kernel(BroadArgs a)
         const int base = a.info ? a.scenes[scene_of(a, m[0])].row_begin : 0;
         if (threadIdx.x == 0) pyset_order<BIG_TAB>(m, k, o, tab, used, tmp, used2, base);
         __syncwarp();
-        for (int j = threadIdx.x; j < k; j += 32) a.sorted[s + j] = o[j];
+        for (int j = threadIdx.x; j < k; j += 32) place(a, s + j, o[j], g);
         __syncwarp();
     }
 }
@@ -317,18 +328,27 @@ __global__ void pairs_kernel(BroadArgs a)
         return;
     }
     const int r = a.sorted[t];
-    const int g = a.cell_of[r];
+    const bool cull = a.cull && a.sorted_pos;
+    const int g = a.sorted_cell ? a.sorted_cell[t] : a.cell_of[r];
     const mwd_scene& sc = a.scenes[scene_of(a, r)];
     int c = 0;
     int64_t out = 0;
     int32_t* pairs = a.pairs;
     const int64_t cap = a.pair_cap;
     if (EMIT) out = a.pair_count[t];
-    const double4* P4 = reinterpret_cast<const double4*>(a.pos);
-    const double4 pr4 = a.cull ? P4[r] : make_double4(0, 0, 0, 0);
-    auto put = [&](int A, int B) {
+    const float4 me = cull ? a.sorted_pos[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+    // B at sorted position j (-1: a wall row given by B alone)
+    auto put = [&](int A, int B, int j) {
         // optional exact-outcome filter: pairs the reference's GJK rejects at its first test
-        if (a.cull && spheres_apart(pr4, P4[B])) return;
+        if (cull) {
+            float4 pb;
+            if (j >= 0) pb = a.sorted_pos[j];
+            else {
+                const double4 w = reinterpret_cast<const double4*>(a.pos)[B];
+                pb = make_float4((float)w.x, (float)w.y, (float)w.z, (float)w.w);
+            }
+            if (spheres_apart_f(me, pb)) return;
+        }
         if (EMIT) {
             if (out < cap) reinterpret_cast<int2*>(pairs)[out] = make_int2(A, B);
             ++out;
@@ -343,12 +363,12 @@ __global__ void pairs_kernel(BroadArgs a)
             const dpos wc = reinterpret_cast<const dpos*>(a.pos)[k];
             const dpos wn = reinterpret_cast<const dpos*>(a.wall_normal)[k];
             double s = wn.x * (p.x - wc.x) + wn.y * (p.y - wc.y) + wn.z * (p.z - wc.z);
-            if (fabs(s) < sc.wall_range) put(r, k);
+            if (fabs(s) < sc.wall_range) put(r, k, -1);
         }
     }
     // later members of the same cell, in set order
     const int cs = a.cell_start[g], ce = a.cell_start[g + 1];
-    for (int j = t + 1; j < ce; ++j) put(r, a.sorted[j]);
+    for (int j = t + 1; j < ce; ++j) put(r, a.sorted[j], j);
     (void)cs;
     // forward neighbours
     const int64_t local = (int64_t)g - sc.cell_base;
@@ -360,7 +380,7 @@ __global__ void pairs_kernel(BroadArgs a)
         if (l2 < 0 || l2 >= sc.n_keys) continue;
         const int g2 = (int)(sc.cell_base + l2);
         const int s2 = a.cell_start[g2], e2 = a.cell_start[g2 + 1];
-        for (int j = s2; j < e2; ++j) put(r, a.sorted[j]);
+        for (int j = s2; j < e2; ++j) put(r, a.sorted[j], j);
     }
     if (!EMIT) a.pair_count[t] = c;
 }

@@ -19,6 +19,8 @@ struct BroadArgs {
     int32_t* cell_of;            // (n,)
     int32_t* scatter_out;        // (n,) rows scattered into their cells (any order within a cell)
     int32_t* sorted;             // (n,) rows in cell order, members in set order
+    float4* sorted_pos;          // (n,) optional: their centres and radii, in the same order
+    int32_t* sorted_cell;        // (n,) with sorted_pos: their cells
     int32_t* pair_count;         // (rows+1,)
     int32_t* scan_tmp;
     int32_t* crowded;            // (crowded_cap,) cells with more than 32 members, this step

@@ -395,6 +395,8 @@ int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_s
     a.total_cells = work->total_cells;
     a.pair_cap = work->pair_cap;
     a.cull = work->cull_pairs ? 1 : 0;
+    a.sorted_pos = reinterpret_cast<float4*>(work->sorted_pos);
+    a.sorted_cell = work->sorted_cell;
     return launch_broad(a, reinterpret_cast<cudaStream_t>(stream));
 }
 

@@ -71,6 +71,16 @@ __device__ __forceinline__ bool spheres_apart(double4 pa, double4 pb)
     return dx * dx + dy * dy + dz * dz > r * r;
 }
 
+// The same test on float copies of the centres (x, y, z, radius): the margin is far above the
+// float rounding of the coordinates (6e-8 relative against 1e-5 of the magnitude).
+__device__ __forceinline__ bool spheres_apart_f(float4 pa, float4 pb)
+{
+    const float dx = pb.x - pa.x, dy = pb.y - pa.y, dz = pb.z - pa.z;
+    const float mag = fmaxf(fmaxf(fabsf(pa.x), fabsf(pa.y)), fabsf(pa.z)) + fmaxf(fmaxf(fabsf(pb.x), fabsf(pb.y)), fabsf(pb.z));
+    const float r = (pa.w + pb.w) * 1.001f + 1e-5f * mag + 1e-6f;
+    return dx * dx + dy * dy + dz * dz > r * r;
+}
+
 __device__ __forceinline__ void set_status(uint32_t* st, uint32_t bits)
 {
     if (st && bits) atomicOr(st, bits);

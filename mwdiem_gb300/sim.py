@@ -215,6 +215,10 @@ class Simulator:
             wk.epa_rec = w["epa_rec"].data_ptr()
             wk.epa_cap = cap
         wk.cull_pairs = 1 if self.cull_pairs else 0
+        w["sorted_pos"] = torch.zeros((n, 4), dtype=torch.float32, device=self.device)
+        w["sorted_cell"] = torch.zeros(n, **i32)
+        wk.sorted_pos = w["sorted_pos"].data_ptr()
+        wk.sorted_cell = w["sorted_cell"].data_ptr()
         wk.total_cells = self.total_cells
         wk.pair_cap = cap
         self.work = wk
