@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-breakdown", action="store_true")
     ap.add_argument("--pairs", type=int, default=1 << 22,
                     help="also time the narrow phase on this many independent random pairs (0: skip)")
+    ap.add_argument("--pairs-only", action="store_true", help="only the independent-pair narrow-phase timing")
     return ap.parse_args()
 
 
@@ -72,7 +73,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                                          "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                          "-lms", "20", "-i", str(self.index)], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -167,6 +168,9 @@ def main():
             return 0
         return reference_arm(args)
     torch.cuda.set_device(local)
+    if args.pairs_only:
+        print(json.dumps({"narrow_pairs": pairs_rate(args.pairs, args.lanes)}), flush=True)
+        return 0
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from mwdiem_gb300 import _lib
@@ -177,14 +181,22 @@ def main():
     V = sim.max_verts
     sim.capture(steps_per_replay=1)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
-    for _ in range(max(3, args.warmup)):
+    # clocks are sampled every 20 ms from the start of the warm-up (kept under the same load for at
+    # least 0.5 s, so the sampler is running) to the end of the timed region
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_warm = time.perf_counter()
+    done = 0
+    while done < max(3, args.warmup) or time.perf_counter() - t_warm < 0.5:
+        flush.zero_()
         sim.replay(1)
+        done += 1
+        if done % 20 == 0:
+            torch.cuda.synchronize()
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks = ClockSampler(local)
-    clocks.start()
     stream = torch.cuda.current_stream()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for i in range(args.steps):
