@@ -51,6 +51,10 @@ def parse():
     ap.add_argument("--pairs", type=int, default=1 << 22,
                     help="also time the narrow phase on this many independent random pairs (0: skip)")
     ap.add_argument("--pairs-only", action="store_true", help="only the independent-pair narrow-phase timing")
+    ap.add_argument("--batch-compare", action="store_true",
+                    help="256 independent scenes (~2M particles): one batched graph step vs per-scene launches")
+    ap.add_argument("--batch-scenes", type=int, default=256)
+    ap.add_argument("--batch-total", type=int, default=2_000_000)
     return ap.parse_args()
 
 
@@ -171,6 +175,9 @@ def main():
     if args.pairs_only:
         print(json.dumps({"narrow_pairs": pairs_rate(args.pairs, args.lanes)}), flush=True)
         return 0
+    if args.batch_compare:
+        print(json.dumps({"batch": batch_compare(args)}), flush=True)
+        return 0
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from mwdiem_gb300 import _lib
@@ -179,6 +186,8 @@ def main():
     spec = build_scene(seed=SCENE["seed"] + rank)
     sim = Simulator(spec, lanes=args.lanes)
     V = sim.max_verts
+    from mwdiem_gb300 import autotune
+    tuning = autotune.tune_lanes(sim, steps=3)
     sim.capture(steps_per_replay=1)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     # clocks are sampled every 20 ms from the start of the warm-up (kept under the same load for at
@@ -241,10 +250,12 @@ def main():
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "particles": N_PARTICLES, "walls": spec.n_walls,
-                       "candidate_pairs_per_step": n_pairs, "lanes_per_pair": args.lanes, "cuda_graph": True,
+                       "candidate_pairs_per_step": n_pairs, "lanes_per_pair": autotune.describe(sim.lanes),
+                       "lanes_tuning_ms": {autotune.describe(k): v for k, v in tuning.items()}, "cuda_graph": True,
                        "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
             "e2e": e2e, "gpu_launches": KERNELS_PER_STEP * args.steps, "clocks": clk,
-            "status": _lib.status_names(status)}
+            "status": _lib.status_names(status), "nonfinite_rows": sim.nonfinite_rows(),
+            "steps_simulated": sim.steps_done}
 
     if rank == 0 and not args.no_breakdown:
         line["breakdown"], line["roofline"] = breakdown(sim, V, flush)
@@ -329,17 +340,25 @@ def pairs_rate(n_pairs, lanes, reps=5):
     import torch
     from mwdiem_gb300 import _lib
     from mwdiem_gb300.pairbench import PairScene
+    from mwdiem_gb300 import autotune
     ps = PairScene(n_pairs, seed=1, lanes=lanes)
-    ps.narrow()
-    torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(reps):
+    sweep = {}
+    for cand in (8 | (8 << 8), 8 | (16 << 8), 8 | (32 << 8), 4 | (16 << 8), 16 | (16 << 8)):
+        ps.lanes = cand
         ps.narrow()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / reps
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            ps.narrow()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sweep[autotune.describe(cand)] = e0.elapsed_time(e1) / reps
+    best = min(sweep, key=sweep.get)
+    ms = sweep[best]
+    ps.lanes = [c for c in (8 | (8 << 8), 8 | (16 << 8), 8 | (32 << 8), 4 | (16 << 8), 16 | (16 << 8))
+                if autotune.describe(c) == best][0]
     ps.narrow(count_work=True)
     torch.cuda.synchronize()
     dots, faces, queries = (int(x) for x in ps.w["counters"].cpu().numpy())
@@ -351,10 +370,61 @@ def pairs_rate(n_pairs, lanes, reps=5):
     ach = flops / (ms * 1e-3) / 1e12
     return {"pairs": n_pairs, "ms_per_launch": ms, "pairs_per_s": n_pairs / (ms * 1e-3),
             "contact_fraction": float((coll == 1).mean()), "support_queries": queries, "vertex_dots": dots,
-            "epa_faces": faces, "lanes_per_pair": lanes, "two_pass": True,
+            "epa_faces": faces, "lanes_per_pair": best, "lanes_sweep_ms": sweep, "two_pass": True,
             "roofline": {"kernel": "gjk_pass + epa_pass", "bound": "fp32", "achieved": ach, "peak": tf.value,
                          "unit": "TFLOP/s", "frac": ach / tf.value if tf.value else None,
                          "peak_source": "measured in this run (mwd_probe_fp32)"}}
+
+
+def batch_compare(args):
+    """Config 4: independent boxes with log-uniform particle counts (cubes, tetrahedra, hulls), dt 5e-5.
+    Batched = all scenes in one state, one launch per stage, one CUDA graph per step, lanes chosen by
+    the autotuner.  Sequential = one simulator per scene, stepped one after another with plain
+    launches.  Contact sets are compared scene by scene after the first broad phase."""
+    import numpy as np
+    import torch
+    from mwdiem_gb300 import autotune, scene
+    from mwdiem_gb300.sim import Simulator
+    t0 = time.perf_counter()
+    specs = scene.batched_scenes(n_scenes=args.batch_scenes, total=args.batch_total, seed=0)
+    n_total = sum(sp.n_particles for sp in specs)
+    batch = Simulator(specs, lanes=args.lanes)
+    singles = [Simulator(sp, lanes=args.lanes) for sp in specs]
+    build_s = time.perf_counter() - t0
+    # identical contact sets, scene by scene
+    batch.broadphase()
+    bp = batch.pairs().cpu().numpy()
+    same = True
+    for i, one in enumerate(singles):
+        one.broadphase()
+        p1 = one.pairs().cpu().numpy()
+        r0, r1 = batch.layout.row_begin[i], batch.layout.row_end[i]
+        mine = bp[(bp[:, 0] >= r0) & (bp[:, 0] < r1)] - r0
+        if set(map(tuple, mine.tolist())) != set(map(tuple, p1.tolist())):
+            same = False
+    tune = autotune.tune_lanes(batch, steps=3)
+    K = max(1, args.steps)
+    ms_batch = autotune.time_steps(batch, steps=K, reps=3)
+    stream = torch.cuda.current_stream()
+    for one in singles:
+        one.lanes = batch.lanes
+        one.step(1)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(K):
+        for one in singles:
+            one.step(1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_seq = e0.elapsed_time(e1) / K
+    return {"scenes": len(specs), "particles": int(n_total), "counts_min_max": [int(min(sp.n_particles for sp in specs)),
+            int(max(sp.n_particles for sp in specs))], "build_s": build_s, "lanes_tuning_ms": tune,
+            "lanes": batch.lanes, "ms_per_step_batched": ms_batch, "ms_per_step_sequential": ms_seq,
+            "particle_steps_per_s_batched": n_total / (ms_batch * 1e-3),
+            "particle_steps_per_s_sequential": n_total / (ms_seq * 1e-3),
+            "batched_over_sequential": ms_seq / ms_batch, "identical_contact_sets": same,
+            "status": batch.status(), "pairs_batched": int(len(bp))}
 
 
 def reference_arm(args):

@@ -260,7 +260,9 @@ int64_t mwd_scan_tmp_ints(int64_t n);
 int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes_host,
                    int32_t n_scenes, mwd_work* work, mwd_stream_t stream);
 
-/* Narrow phase + force over work->pairs[0 .. *work->n_pairs) into st->force/torque. */
+/* Narrow phase + force over work->pairs[0 .. *work->n_pairs) into st->force/torque.
+ * lanes: lanes per pair of the GJK pass (4, 8, 16, 32), plus, in bits 8-15, those of the EPA pass
+ * of the two-pass kernel (0: the same). */
 int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work* work,
                      int32_t lanes, mwd_stream_t stream);
 

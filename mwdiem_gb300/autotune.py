@@ -1,0 +1,59 @@
+"""Autotuner for the device-resident step.
+
+Chooses the lanes per pair of the narrow phase's GJK pass and EPA pass (4, 8, 16 or 32 lanes per
+pair, i.e. 8, 4, 2 or 1 pairs per warp) by timing graph-captured steps of the actual scene and
+keeping the fastest.  The
+cell size is not a tuning knob: it decides the reference's candidate set (an 8-cell forward stencil
+misses some neighbour pairs, and which ones depends on the cell size), so it stays what the scene
+defines (MWDiem.py:575-580).
+"""
+from __future__ import annotations
+
+import copy
+
+import torch
+
+
+def time_steps(sim, steps=5, reps=3):
+    """Median ms per graph-replayed step (after one captured warm-up step)."""
+    sim.capture(1)
+    stream = torch.cuda.current_stream()
+    best = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.replay(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        best.append(e0.elapsed_time(e1) / steps)
+    best.sort()
+    return best[len(best) // 2]
+
+
+DEFAULT_CANDIDATES = tuple(g | (e << 8) for g in (4, 8, 16) for e in (8, 16, 32))
+
+
+def describe(lanes):
+    return f"gjk{lanes & 0xff}/epa{((lanes >> 8) & 0xff) or (lanes & 0xff)}"
+
+
+def tune_lanes(sim, candidates=DEFAULT_CANDIDATES, steps=5):
+    """Time the scene with each lanes-per-pair setting (GJK-pass lanes | EPA-pass lanes << 8) on a
+    copy of its state, set the fastest on `sim`, and return {setting: ms per step}.  The state of
+    `sim` is restored afterwards."""
+    saved = {k: v.clone() for k, v in sim.t.items()}
+    res = {}
+    for lanes in candidates:
+        sim.lanes = int(lanes)
+        sim.graph = None
+        res[lanes] = time_steps(sim, steps)
+        for k, v in saved.items():
+            sim.t[k].copy_(v)
+    best = min(res, key=res.get)
+    sim.lanes = int(best)
+    sim.graph = None
+    for k, v in saved.items():
+        sim.t[k].copy_(v)
+    sim.w["status"].zero_()
+    torch.cuda.synchronize()
+    return res

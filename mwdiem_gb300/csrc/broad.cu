@@ -374,14 +374,20 @@ __global__ void pairs_kernel(BroadArgs a)
     const int64_t local = (int64_t)g - sc.cell_base;
     const int64_t nx = sc.nx, nxy = sc.nx * sc.ny;
     const int64_t offs[7] = {1, nx, nxy, nxy + 1, nxy + 1 + nx, nxy + nx, nx + 1};
+    // the 7 neighbour ranges are loaded first (independent loads), then walked
+    int rs[7], re[7];
 #pragma unroll
     for (int o = 0; o < 7; ++o) {
         const int64_t l2 = local + offs[o];
+        rs[o] = re[o] = 0;
         if (l2 < 0 || l2 >= sc.n_keys) continue;
         const int g2 = (int)(sc.cell_base + l2);
-        const int s2 = a.cell_start[g2], e2 = a.cell_start[g2 + 1];
-        for (int j = s2; j < e2; ++j) put(r, a.sorted[j], j);
+        rs[o] = a.cell_start[g2];
+        re[o] = a.cell_start[g2 + 1];
     }
+#pragma unroll
+    for (int o = 0; o < 7; ++o)
+        for (int j = rs[o]; j < re[o]; ++j) put(r, a.sorted[j], j);
     if (!EMIT) a.pair_count[t] = c;
 }
 

@@ -412,8 +412,9 @@ int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work*
         return MWD_ERR_UNSUPPORTED;
     }
     int lp;
-    int rc = check_lanes(lanes, &lp);
+    int rc = check_lanes(lanes & 0xff, &lp);
     if (rc) return rc;
+    const int elp = (lanes >> 8) & 0xff;
     NarrowArgs a = {};
     a.st = *st;
     a.scenes = scenes_dev;
@@ -429,7 +430,7 @@ int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work*
         a.epa_rec = work->epa_rec;
         a.epa_cap = work->epa_cap;
         a.pre_culled = work->cull_pairs ? 1 : 0;
-        return launch_narrow_two_pass(a, lp, reinterpret_cast<cudaStream_t>(stream));
+        return launch_narrow_two_pass(a, lp | (elp << 8), reinterpret_cast<cudaStream_t>(stream));
     }
     return launch_narrow(a, 1, lp, -1, reinterpret_cast<cudaStream_t>(stream));
 }

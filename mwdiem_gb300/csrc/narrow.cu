@@ -879,10 +879,10 @@ __global__ void __launch_bounds__(NARROW_THREADS) epa_pass_kernel(NarrowArgs a)
     }
 }
 
-template <int LPP>
+template <int LPP, int ELPP>
 int launch_two_pass_lpp(const NarrowArgs& a, cudaStream_t s)
 {
-    constexpr int GPB = NARROW_THREADS / LPP;
+    constexpr int GPB = NARROW_THREADS / ELPP;
     // occupancy queried once per (kernel, shared-memory size); no runtime calls during capture after that
     static int gjk_per_sm = 0;
     static size_t epa_shm_cached = 0;
@@ -895,18 +895,18 @@ int launch_two_pass_lpp(const NarrowArgs& a, cudaStream_t s)
     }
     const size_t shm = (size_t)GPB * sizeof(EpaMem) + (size_t)GPB * 2 * a.hull_cap * sizeof(float4);
     if (!attr) {
-        MWD_CUDA(cudaFuncSetAttribute(epa_pass_kernel<LPP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        MWD_CUDA(cudaFuncSetAttribute(epa_pass_kernel<ELPP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         attr = true;
     }
     if (shm != epa_shm_cached || !epa_per_sm) {
         int v = 0;
-        MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, epa_pass_kernel<LPP>, NARROW_THREADS, shm));
+        MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, epa_pass_kernel<ELPP>, NARROW_THREADS, shm));
         epa_per_sm = v < 1 ? 1 : v;
         epa_shm_cached = shm;
     }
     MWD_CUDA(cudaMemsetAsync(a.epa_count, 0, sizeof(int32_t), s));
     gjk_pass_kernel<LPP><<<(unsigned)(num_sms() * gjk_per_sm), NARROW_THREADS, 0, s>>>(a);
-    epa_pass_kernel<LPP><<<(unsigned)(num_sms() * epa_per_sm), NARROW_THREADS, shm, s>>>(a);
+    epa_pass_kernel<ELPP><<<(unsigned)(num_sms() * epa_per_sm), NARROW_THREADS, shm, s>>>(a);
     MWD_CUDA(cudaGetLastError());
     return MWD_OK;
 }
@@ -985,15 +985,19 @@ int launch_narrow(const NarrowArgs& a, int mode, int lanes, int64_t n_hint, cuda
     return MWD_ERR_INVALID;
 }
 
+// lanes = GJK-pass lanes per pair | EPA-pass lanes per pair << 8 (EPA lanes 0: same as GJK)
 int launch_narrow_two_pass(const NarrowArgs& a, int lanes, cudaStream_t s)
 {
-    switch (lanes) {
-        case 4: return launch_two_pass_lpp<4>(a, s);
-        case 8: return launch_two_pass_lpp<8>(a, s);
-        case 16: return launch_two_pass_lpp<16>(a, s);
-        case 32: return launch_two_pass_lpp<32>(a, s);
-    }
-    set_error("lanes per pair must be 4, 8, 16 or 32 (got %d)", lanes);
+    const int gl = lanes & 0xff;
+    int el = (lanes >> 8) & 0xff;
+    if (!el) el = gl;
+#define MWD_TP(G, E) if (gl == G && el == E) return launch_two_pass_lpp<G, E>(a, s)
+    MWD_TP(4, 4); MWD_TP(4, 8); MWD_TP(4, 16); MWD_TP(4, 32);
+    MWD_TP(8, 8); MWD_TP(8, 16); MWD_TP(8, 32); MWD_TP(8, 4);
+    MWD_TP(16, 16); MWD_TP(16, 32); MWD_TP(16, 8); MWD_TP(16, 4);
+    MWD_TP(32, 32); MWD_TP(32, 16); MWD_TP(32, 8); MWD_TP(32, 4);
+#undef MWD_TP
+    set_error("lanes per pair must be 4, 8, 16 or 32 (got GJK %d, EPA %d)", gl, el);
     return MWD_ERR_INVALID;
 }
 

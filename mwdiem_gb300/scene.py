@@ -36,6 +36,27 @@ class Body:
 
 
 @dataclass
+class CompactBodies:
+    """Particles drawn from a pool of shapes: particle k is pool[pick[k]] rotated by quats[k]
+    (orientation baked into its vertices, quaternion state starting at identity).  Builds large
+    scenes without one Python object per particle."""
+    pool: list
+    pick: np.ndarray
+    quats: np.ndarray
+
+    def __len__(self):
+        return int(len(self.pick))
+
+    def expand(self):
+        out = []
+        for k in range(len(self.pick)):
+            b = self.pool[int(self.pick[k])]
+            out.append(Body(vertices=b.vertices @ shapes.quat_to_matrix(self.quats[k]).T, inertia_bf=b.inertia_bf,
+                            inertia_size=b.inertia_size, mass=b.mass))
+        return out
+
+
+@dataclass
 class SceneSpec:
     """Host description of one scene (rows: walls, then particles)."""
     walls: list = field(default_factory=list)          # list of (Body, centre (3,), normal (3,))
@@ -62,6 +83,9 @@ class SceneSpec:
     @property
     def n_particles(self) -> int:
         return len(self.bodies)
+
+    def body_list(self):
+        return self.bodies.expand() if isinstance(self.bodies, CompactBodies) else list(self.bodies)
 
     def wall_bbox(self):
         lo = np.full(3, np.inf)
@@ -253,12 +277,9 @@ def batched_scenes(n_scenes=256, total=2_000_000, n_lo=100, n_hi=50_000, seed=0,
         height = float(centres[:, 2].max() + spacing + 4.8)
         walls = box_walls(side, side, height, 24.0)
         pick = rng.integers(len(base), size=int(n))
-        bodies = []
-        for k in range(int(n)):
-            b = base[pick[k]]
-            q = shapes.random_quaternion(rng)
-            bodies.append(Body(vertices=b.vertices @ shapes.quat_to_matrix(q).T, inertia_bf=b.inertia_bf,
-                               inertia_size=b.inertia_size, mass=b.mass))
+        q = rng.normal(size=(int(n), 4))
+        q /= np.linalg.norm(q, axis=1, keepdims=True)
+        bodies = CompactBodies(pool=base, pick=pick, quats=q)
         scenes.append(SceneSpec(walls=walls, bodies=bodies, centres=centres, velocities=np.zeros((int(n), 3)),
                                 Kn=kn, en=en, et=en, mu=mu, Kn_wall=kn, en_wall=en, et_wall=en, mu_wall=mu, dt=dt,
                                 max_particlesize=2.4, name=f"batch{s}"))

@@ -17,7 +17,7 @@ import torch
 from . import _dev
 from ._lib import (HULL_CAP, ST_PAIR_OVERFLOW, ContactParams, Material, MwdError, Scene, State, Work, check, lib,
                    status_names)
-from .scene import SceneSpec
+from .scene import CompactBodies, SceneSpec
 
 _STATE_F64 = ("pos", "dx_all", "wall_normal")
 _STATE_F32 = ("vel", "vel_half", "w_half_bf", "w_bf", "w", "q", "q_half", "q_all", "q_acc", "force", "torque",
@@ -55,92 +55,147 @@ class Simulator:
 
     # ------------------------------------------------------------------ set-up
     def _build_state(self):
-        rows_pos, rows_nrm, rows_vel, rows_inertia, rows_inv, rows_ext, info = [], [], [], [], [], [], []
-        verts, counts = [], []
+        """Row arrays of every scene (walls, then particles), concatenated; vertex tables in CSR.
+        Explicit bodies are assembled on the host; CompactBodies are rotated on the device."""
+        dev = self.device
+        parts = []          # per scene: dict of row arrays
+        explicit = []       # (global row, vertices (k,3))
+        compact = []        # (global rows (m,), pool id, pick (m,), quats (m,4))
+        pools = {}
         rb, we, re = [], [], []
         row = 0
         for s_id, sp in enumerate(self.specs):
             rb.append(row)
-            for b, c, nrm in sp.walls:
-                rows_pos.append(c)
-                rows_nrm.append(nrm)
-                rows_vel.append(np.zeros(3))
-                I = np.asarray(b.inertia_bf, dtype=np.float64)
-                rows_inertia.append([I[0], I[1], I[2], b.inertia_size])
-                rows_inv.append([1 / I[0], 1 / I[1], 1 / I[2], 1 / b.mass])
-                rows_ext.append(np.zeros(3))
-                info.append((s_id << 1) | 1)
-                verts.append(b.vertices)
-                counts.append(b.vertices.shape[0])
-                row += 1
-            we.append(row)
+            W = len(sp.walls)
+            n_p = sp.n_particles
             g = np.asarray(sp.gravity, dtype=np.float64)
-            vel = sp.velocities if sp.velocities is not None else np.zeros((sp.n_particles, 3))
-            for k, b in enumerate(sp.bodies):
-                rows_pos.append(sp.centres[k])
-                rows_nrm.append(np.zeros(3))
-                rows_vel.append(vel[k])
-                I = np.asarray(b.inertia_bf, dtype=np.float64)
-                rows_inertia.append([I[0], I[1], I[2], b.inertia_size])
-                rows_inv.append([1 / I[0], 1 / I[1], 1 / I[2], 1 / b.mass])
-                rows_ext.append(b.mass * g)
-                info.append(s_id << 1)
-                verts.append(b.vertices)
-                counts.append(b.vertices.shape[0])
-                row += 1
+            wall_I = np.array([np.asarray(b.inertia_bf, float) for b, _, _ in sp.walls]).reshape(W, 3)
+            wall_size = np.array([b.inertia_size for b, _, _ in sp.walls])
+            wall_mass = np.array([b.mass for b, _, _ in sp.walls])
+            wall_cnt = np.array([b.vertices.shape[0] for b, _, _ in sp.walls], dtype=np.int64)
+            wall_rad = np.array([np.sqrt((b.vertices.astype(np.float32).astype(np.float64) ** 2).sum(1)).max()
+                                 for b, _, _ in sp.walls])
+            for k, (b, _, _) in enumerate(sp.walls):
+                explicit.append((row + k, b.vertices))
+            cb = sp.bodies
+            if isinstance(cb, CompactBodies):
+                key = id(cb.pool)
+                if key not in pools:
+                    pools[key] = cb.pool
+                pick = np.asarray(cb.pick, dtype=np.int64)
+                pm = np.array([b.mass for b in cb.pool])
+                pI = np.array([np.asarray(b.inertia_bf, float) for b in cb.pool])
+                ps = np.array([b.inertia_size for b in cb.pool])
+                pc = np.array([b.vertices.shape[0] for b in cb.pool], dtype=np.int64)
+                pr = np.array([np.sqrt((b.vertices.astype(np.float32).astype(np.float64) ** 2).sum(1)).max()
+                               for b in cb.pool])
+                p_mass, p_I, p_size, p_cnt, p_rad = pm[pick], pI[pick], ps[pick], pc[pick], pr[pick]
+                compact.append((np.arange(row + W, row + W + n_p), key, pick, np.asarray(cb.quats, float)))
+            else:
+                bl = list(cb)
+                p_mass = np.array([b.mass for b in bl])
+                p_I = np.array([np.asarray(b.inertia_bf, float) for b in bl]).reshape(n_p, 3)
+                p_size = np.array([b.inertia_size for b in bl])
+                p_cnt = np.array([b.vertices.shape[0] for b in bl], dtype=np.int64)
+                p_rad = np.array([np.sqrt((b.vertices.astype(np.float32).astype(np.float64) ** 2).sum(1)).max()
+                                  for b in bl])
+                for k, b in enumerate(bl):
+                    explicit.append((row + W + k, b.vertices))
+            vel = sp.velocities if sp.velocities is not None else np.zeros((n_p, 3))
+            parts.append(dict(
+                pos=np.concatenate([np.array([c for _, c, _ in sp.walls]).reshape(W, 3), np.asarray(sp.centres)]),
+                nrm=np.concatenate([np.array([nn for _, _, nn in sp.walls]).reshape(W, 3), np.zeros((n_p, 3))]),
+                vel=np.concatenate([np.zeros((W, 3)), np.asarray(vel, float)]),
+                I=np.concatenate([wall_I, p_I]), size=np.concatenate([wall_size, p_size]),
+                mass=np.concatenate([wall_mass, p_mass]),
+                ext=np.concatenate([np.zeros((W, 3)), p_mass[:, None] * g[None, :]]),
+                info=np.concatenate([np.full(W, (s_id << 1) | 1), np.full(n_p, s_id << 1)]).astype(np.int32),
+                cnt=np.concatenate([wall_cnt, p_cnt]), rad=np.concatenate([wall_rad, p_rad])))
+            row += W
+            we.append(row)
+            row += n_p
             re.append(row)
         n = row
         self.layout = Layout(rb, we, re)
         self.n = n
-        counts = np.asarray(counts, dtype=np.int64)
+        cat = {k: np.concatenate([pt[k] for pt in parts]) for k in parts[0]}
+        counts = cat["cnt"].astype(np.int64)
         if counts.max() > HULL_CAP:
             raise ValueError(f"a shape has {counts.max()} vertices; the narrow phase stages at most {HULL_CAP}")
         off = np.zeros(n + 1, dtype=np.int64)
         np.cumsum(counts, out=off[1:])
         self.vert_off_host = off
         self.max_verts = int(counts.max())
-        bv = np.zeros((int(off[-1]), 4), dtype=np.float32)
-        bv[:, :3] = np.concatenate(verts, 0)
+        total = int(off[-1])
+        f32 = dict(dtype=torch.float32, device=dev)
+        off_d = torch.from_numpy(off).to(dev)
+        counts_d = torch.from_numpy(counts).to(dev)
+        body = torch.zeros((total, 4), **f32)
+        if explicit:
+            rows_e = np.array([r for r, _ in explicit], dtype=np.int64)
+            vals = np.concatenate([v for _, v in explicit], 0).astype(np.float32)
+            idx = _ranges(off_d[torch.from_numpy(rows_e).to(dev)], counts_d[torch.from_numpy(rows_e).to(dev)])
+            body[idx, :3] = torch.from_numpy(vals).to(dev)
+        for rows_c, key, pick, quats in compact:
+            pool = pools[key]
+            Vp = max(b.vertices.shape[0] for b in pool)
+            pv = np.zeros((len(pool), Vp, 3), np.float32)
+            for i, b in enumerate(pool):
+                pv[i, :b.vertices.shape[0]] = b.vertices
+            pv_d = torch.from_numpy(pv).to(dev)
+            rows_t = torch.from_numpy(rows_c).to(dev)
+            pick_t = torch.from_numpy(pick).to(dev)
+            q_t = torch.from_numpy(quats.astype(np.float32)).to(dev)
+            chunk = 1 << 18
+            for a0 in range(0, len(rows_c), chunk):
+                a1 = min(len(rows_c), a0 + chunk)
+                R = _quat_to_matrix(q_t[a0:a1])
+                v = torch.einsum("rij,rkj->rki", R, pv_d[pick_t[a0:a1]])
+                c = counts_d[rows_t[a0:a1]]
+                mask = torch.arange(Vp, device=dev)[None, :] < c[:, None]
+                idx = _ranges(off_d[rows_t[a0:a1]], c)
+                body[idx, :3] = v[mask]
         pos = np.zeros((n, 4))
-        pos[:, :3] = np.asarray(rows_pos)
-        # bounding radius of each row (used by the narrow phase's sphere pre-test)
-        pos[:, 3] = [float(np.sqrt((v.astype(np.float32).astype(np.float64) ** 2).sum(1)).max()) for v in verts]
-        f32 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(self.device)  # noqa: E731
-        f64 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(self.device)  # noqa: E731
-        z4 = np.zeros((n, 4))
-        qid = np.tile([1.0, 0.0, 0.0, 0.0], (n, 1))
-        vel4 = np.zeros((n, 4))
-        vel4[:, :3] = np.asarray(rows_vel)
-        nrm4 = np.zeros((n, 4))
-        nrm4[:, :3] = np.asarray(rows_nrm)
-        ext4 = np.zeros((n, 4))
-        ext4[:, :3] = np.asarray(rows_ext)
+        pos[:, :3] = cat["pos"]
+        pos[:, 3] = cat["rad"]  # bounding radius (used by the narrow phase's sphere test)
+        I = cat["I"]
+        inertia = np.concatenate([I, cat["size"][:, None]], 1)
+        inv = np.concatenate([1.0 / I, 1.0 / cat["mass"][:, None]], 1)
+        z4 = torch.zeros((n, 4), **f32)
         t = {}
-        t["pos"] = f64(pos)
-        t["dx_all"] = f64(z4)
-        t["wall_normal"] = f64(nrm4)
-        t["vel"] = f32(vel4)
-        t["vel_half"] = f32(vel4)
+        t["pos"] = torch.from_numpy(pos).to(dev)
+        t["dx_all"] = torch.zeros((n, 4), dtype=torch.float64, device=dev)
+        nrm4 = np.zeros((n, 4))
+        nrm4[:, :3] = cat["nrm"]
+        t["wall_normal"] = torch.from_numpy(nrm4).to(dev)
+        vel4 = np.zeros((n, 4), np.float32)
+        vel4[:, :3] = cat["vel"]
+        t["vel"] = torch.from_numpy(vel4).to(dev)
+        t["vel_half"] = t["vel"].clone()
         for k in ("w_half_bf", "w_bf", "w", "force", "torque", "ext_torque"):
-            t[k] = f32(z4)
+            t[k] = z4.clone()
+        qid = torch.zeros((n, 4), **f32)
+        qid[:, 0] = 1.0
         for k in ("q", "q_half", "q_all", "q_acc"):
-            t[k] = f32(qid)
-        t["ext_force"] = f32(ext4)
-        t["inertia"] = f32(np.asarray(rows_inertia))
-        t["inv_inertia"] = f32(np.asarray(rows_inv))
-        t["info"] = torch.from_numpy(np.asarray(info, dtype=np.int32)).to(self.device)
-        t["vert_off"] = torch.from_numpy(off.astype(np.int32)).to(self.device)
-        t["body_verts"] = f32(bv)
-        wv = bv.copy()
-        owner = np.repeat(np.arange(n), counts)
-        wv[:, :3] = (pos[owner, :3] + bv[:, :3].astype(np.float64)).astype(np.float32)
-        t["world_verts"] = f32(wv)
+            t[k] = qid.clone()
+        ext4 = np.zeros((n, 4), np.float32)
+        ext4[:, :3] = cat["ext"]
+        t["ext_force"] = torch.from_numpy(ext4).to(dev)
+        t["inertia"] = torch.from_numpy(inertia.astype(np.float32)).to(dev)
+        t["inv_inertia"] = torch.from_numpy(inv.astype(np.float32)).to(dev)
+        t["info"] = torch.from_numpy(cat["info"]).to(dev)
+        t["vert_off"] = off_d.to(torch.int32)
+        t["body_verts"] = body
+        owner = torch.repeat_interleave(torch.arange(n, device=dev), counts_d)
+        world = body.clone()
+        world[:, :3] = (t["pos"][owner, :3] + body[:, :3].double()).float()
+        t["world_verts"] = world
         self.t = t
         st = State()
         for k in _STATE_F64 + _STATE_F32 + ("info", "vert_off", "body_verts", "world_verts"):
             setattr(st, k, t[k].data_ptr())
         st.n = n
-        st.n_verts = int(off[-1])
+        st.n_verts = total
         st.max_verts = self.max_verts
         self.state = st
 
@@ -307,6 +362,12 @@ class Simulator:
             raise MwdError(3, f"pair buffer overflow (capacity {self.pair_cap}); status {status_names(st)}")
         return st
 
+    def nonfinite_rows(self) -> int:
+        """Rows whose centre or velocity is not finite (they drop out of the cell table)."""
+        p = self.t["pos"][:, :3]
+        v = self.t["vel"][:, :3]
+        return int((~torch.isfinite(p).all(1) | ~torch.isfinite(v).all(1)).sum().item())
+
     def n_pairs(self) -> int:
         return int(self.w["n_pairs"].item())
 
@@ -340,3 +401,21 @@ class Simulator:
                  wbf=t["w_bf"][:, :3].astype(np.float64), w=t["w"][:, :3].astype(np.float64),
                  q=t["q"].astype(np.float64), q12=t["q_half"].astype(np.float64), qall=t["q_all"].astype(np.float64))
         return d
+
+
+def _ranges(starts, counts):
+    """Concatenation of arange(starts[i], starts[i] + counts[i]) (device tensors)."""
+    total = int(counts.sum().item())
+    if total == 0:
+        return torch.zeros(0, dtype=torch.int64, device=starts.device)
+    rep_start = torch.repeat_interleave(starts, counts)
+    first = torch.cumsum(counts, 0) - counts
+    within = torch.arange(total, device=starts.device) - torch.repeat_interleave(first, counts)
+    return rep_start + within
+
+
+def _quat_to_matrix(q):
+    w, x, y, z = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    return torch.stack([torch.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)], 1),
+                        torch.stack([2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)], 1),
+                        torch.stack([2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], 1)], 1)

@@ -23,7 +23,7 @@ class RefStepper:
     def __init__(self, spec, V=None, kind="port", nthreads=1):
         """spec: mwdiem_gb300.scene.SceneSpec (walls first, then particles)."""
         W = spec.n_walls
-        bodies = [b for b, _, _ in spec.walls] + list(spec.bodies)
+        bodies = [b for b, _, _ in spec.walls] + spec.body_list()
         centres = np.concatenate([np.array([c for _, c, _ in spec.walls]).reshape(-1, 3), spec.centres], 0)
         N = len(bodies)
         nv = np.array([b.vertices.shape[0] for b in bodies], dtype=np.int32)
