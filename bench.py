@@ -35,7 +35,8 @@ WORKLOAD = ("pour20k: 20,000 convex hulls of U{12..32} points on a sphere of rad
             "lattice (spacing 2.6) in a 40x40 box, random orientations, at rest, gravity; kn 1e5, damping "
             "ratio 0.3 (en=et=0.372), mu 0.5, dt 5e-5")
 METRIC = "particle-steps/s"
-KERNELS_PER_STEP = 13  # broad phase 10 (assign, 2 scan, scatter, order, crowded, count, 2 scan, emit) + GJK pass + EPA pass + integrate
+WINDOW_STEPS = 500  # the pour configuration runs 500 steps
+KERNELS_PER_STEP = 11  # broad phase 7 (assign, 2 scan, scatter, order, crowded, append) + GJK pass + EPA pass + integrate rows + vertices
 
 
 def parse():
@@ -53,6 +54,11 @@ def parse():
     ap.add_argument("--pairs-only", action="store_true", help="only the independent-pair narrow-phase timing")
     ap.add_argument("--batch-compare", action="store_true",
                     help="256 independent scenes (~2M particles): one batched graph step vs per-scene launches")
+    ap.add_argument("--calibration", action="store_true",
+                    help="differentiable calibration: 2,000 hulls, 5,000 steps, forward vs forward + adjoint")
+    ap.add_argument("--calib-steps", type=int, default=5000)
+    ap.add_argument("--calib-particles", type=int, default=2000)
+    ap.add_argument("--contact-point", default="reference", choices=["reference", "midpoint"])
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--batch-total", type=int, default=2_000_000)
     return ap.parse_args()
@@ -159,6 +165,28 @@ def integrate_bytes(sim):
     return sim.n * (64 + 224 + 8 + 64 + 176) + sim.state.n_verts * 32
 
 
+class Window:
+    """The pour is timed over its first WINDOW_STEPS steps (the configuration's length): the mutable
+    state is restored to the initial state whenever a window ends."""
+
+    def __init__(self, sim, length):
+        self.sim = sim
+        self.length = int(length)
+        self.snap = {k: sim.t[k].clone() for k in sim.MUTABLE + ("force", "torque")}
+        self.pos = 0
+
+    def restore(self):
+        for k, v in self.snap.items():
+            self.sim.t[k].copy_(v)
+        self.sim.w["status"].zero_()
+        self.pos = 0
+
+    def before_step(self):
+        if self.pos >= self.length:
+            self.restore()
+        self.pos += 1
+
+
 def main():
     args = parse()
     import torch
@@ -178,6 +206,9 @@ def main():
     if args.batch_compare:
         print(json.dumps({"batch": batch_compare(args)}), flush=True)
         return 0
+    if args.calibration:
+        print(json.dumps({"calibration": calibration(args)}), flush=True)
+        return 0
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from mwdiem_gb300 import _lib
@@ -186,9 +217,11 @@ def main():
     spec = build_scene(seed=SCENE["seed"] + rank)
     sim = Simulator(spec, lanes=args.lanes)
     V = sim.max_verts
+    window = Window(sim, WINDOW_STEPS)
     from mwdiem_gb300 import autotune
     tuning = autotune.tune_lanes(sim, steps=3)
     sim.capture(steps_per_replay=1)
+    window.restore()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     # clocks are sampled every 20 ms from the start of the warm-up (kept under the same load for at
     # least 0.5 s, so the sampler is running) to the end of the timed region
@@ -198,11 +231,13 @@ def main():
     done = 0
     while done < max(3, args.warmup) or time.perf_counter() - t_warm < 0.5:
         flush.zero_()
+        window.before_step()
         sim.replay(1)
         done += 1
         if done % 20 == 0:
             torch.cuda.synchronize()
     torch.cuda.synchronize()
+    window.restore()
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -210,6 +245,7 @@ def main():
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for i in range(args.steps):
         flush.zero_()
+        window.before_step()
         ev[i][0].record(stream)
         sim.replay(1)
         ev[i][1].record(stream)
@@ -225,9 +261,11 @@ def main():
     total_ms = float(t.item())
     status = sim.check_status()
     n_pairs = sim.n_pairs()
+    nonfinite = sim.nonfinite_rows()
     value = N_PARTICLES * args.steps * world / (total_ms * 1e-3)
 
-    # e2e: state from pinned host memory in, result back out, every step
+    # e2e: state from pinned host memory in, result back out, every step (from the initial state)
+    window.restore()
     host = sim.host_state()
     nbytes = sim.host_state_bytes()
     sim.step_host(host, 1)
@@ -252,12 +290,15 @@ def main():
             "config": {"workload": WORKLOAD, "particles": N_PARTICLES, "walls": spec.n_walls,
                        "candidate_pairs_per_step": n_pairs, "lanes_per_pair": autotune.describe(sim.lanes),
                        "lanes_tuning_ms": {autotune.describe(k): v for k, v in tuning.items()}, "cuda_graph": True,
-                       "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
+                       "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}",
+                       "window": f"steps 0..{WINDOW_STEPS - 1} of the pour from its initial state (the state is "
+                                 f"restored every {WINDOW_STEPS} steps, outside the timed events)"},
             "e2e": e2e, "gpu_launches": KERNELS_PER_STEP * args.steps, "clocks": clk,
-            "status": _lib.status_names(status), "nonfinite_rows": sim.nonfinite_rows(),
+            "status": _lib.status_names(status), "nonfinite_rows": nonfinite,
             "steps_simulated": sim.steps_done}
 
     if rank == 0 and not args.no_breakdown:
+        window.restore()
         line["breakdown"], line["roofline"] = breakdown(sim, V, flush)
     if rank == 0 and args.pairs > 0:
         del sim
@@ -326,7 +367,7 @@ def breakdown(sim, V, flush, reps=10):
         n, P = sim.n, sim.n_pairs()
         bbytes = n * (32 + 4 + 4 + 4 + 4 + 4 + 8) + sim.total_cells * 12 + P * (8 + 8 + 8)
         a = bbytes / (ms["broad"] * 1e-3) / 1e9
-        roof = {"kernel": "broad phase (12 kernels)", "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s",
+        roof = {"kernel": "broad phase (7 kernels)", "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s",
                 "frac": a / hbm, "traffic": None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in pk else "fallback 6800"}
     return out, roof
@@ -425,6 +466,126 @@ def batch_compare(args):
             "particle_steps_per_s_sequential": n_total / (ms_seq * 1e-3),
             "batched_over_sequential": ms_seq / ms_batch, "identical_contact_sets": same,
             "status": batch.status(), "pairs_batched": int(len(bp))}
+
+
+def calibration(args):
+    """Config 5: 2,000 random hulls (12-32 points, radius U[0.8,1.2]) poured in a 20 x 20 box, 5,000
+    steps at dt 5e-5.  Loss = MSE of the per-step centre of mass against a target trajectory of the
+    same simulator with kn 2e5, damping ratio 0.2, mu 0.4; gradients with respect to kn, damping
+    ratio, mu and the initial velocities, checkpoints every 100 steps.  Times the differentiable
+    forward alone and forward + adjoint (CUDA events, same stream), and the plain FP32 step of the
+    same scene; the FP64 finite-difference check runs at 16 particles x 50 steps."""
+    import numpy as np
+    import torch
+    from mwdiem_gb300 import scene
+    from mwdiem_gb300.diff import DiffEngine, law_from, rollout
+    from mwdiem_gb300.sim import Simulator
+    n, steps = args.calib_particles, args.calib_steps
+    spec = scene.pour_scene(n=n, box=20.0, seed=0)
+    eng = DiffEngine(spec, steps, ckpt_every=100, contact_point=args.contact_point)
+    dev = eng.device
+    W = eng.n_walls
+    x0 = eng.initial_state()
+    target, _ = eng.forward(x0, law_from(2e5, 0.2, 0.4).to(dev), steps)
+    st_target = eng.status_word()
+    stream = torch.cuda.current_stream()
+
+    def run(backward):
+        kn = torch.tensor(1e5, dtype=torch.float64, device=dev, requires_grad=True)
+        zeta = torch.tensor(0.3, dtype=torch.float64, device=dev, requires_grad=True)
+        mu = torch.tensor(0.5, dtype=torch.float64, device=dev, requires_grad=True)
+        v0 = torch.zeros((n, 3), dtype=torch.float64, device=dev, requires_grad=True)
+        x = torch.cat([x0[:W], torch.cat([x0[W:, :3], v0, v0, x0[W:, 9:]], 1)], 0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        if backward:
+            com, _ = rollout(eng, x, law_from(kn, zeta, mu).to(dev), steps)
+            loss = ((com - target) ** 2).mean()
+            loss.backward()
+        else:
+            with torch.no_grad():
+                com, _ = rollout(eng, x, law_from(kn, zeta, mu).to(dev), steps)
+                loss = ((com - target) ** 2).mean()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        g = None
+        if backward:
+            g = {"kn": float(kn.grad), "damping": float(zeta.grad), "mu": float(mu.grad),
+                 "v0_norm": float(v0.grad.norm()), "finite": bool(torch.isfinite(v0.grad).all())}
+        return e0.elapsed_time(e1), float(loss), g
+
+    run(False)  # warm-up: graph capture
+    fwd = sorted(run(False)[0] for _ in range(3))[1]
+    fb = []
+    for _ in range(3):
+        ms, loss, grads = run(True)
+        fb.append(ms)
+    fwd_bwd = sorted(fb)[1]
+    contacts = int(eng.step_off[steps].item())
+    st = eng.status_word()
+    # the plain device step of the same scene (FP32 state, CUDA graph)
+    sim = Simulator(spec)
+    sim.capture(1)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.replay(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    from mwdiem_gb300._lib import status_names
+    return {"particles": n, "steps": steps, "checkpoint_every": 100, "contact_point": args.contact_point,
+            "contacts_logged": contacts, "ms_forward": fwd, "ms_forward_adjoint": fwd_bwd,
+            "adjoint_over_forward": fwd_bwd / fwd, "ms_plain_fp32_steps": plain_ms,
+            "forward_over_plain": fwd / plain_ms, "loss": loss, "grads": grads,
+            "status": status_names(st), "status_target": status_names(st_target),
+            "fd_check_16x50": fd_check()}
+
+
+def fd_check(steps=50):
+    """Relative difference between the adjoint gradient and FP64 central differences (h = 1e-6
+    relative) of the whole forward, 16 packed hulls x 50 steps, for kn, damping, mu and a random
+    direction of the initial velocities."""
+    import numpy as np
+    import torch
+    from mwdiem_gb300 import scene
+    from mwdiem_gb300.diff import DiffEngine, law_from, rollout
+    eng = DiffEngine(scene.packed_scene(16, seed=3), steps, ckpt_every=10)
+    dev = eng.device
+    W = eng.n_walls
+    x0 = eng.initial_state()
+    target, _ = eng.forward(x0, law_from(2e5, 0.2, 0.4).to(dev), steps)
+    base = {"kn": 1e5, "zeta": 0.3, "mu": 0.5}
+    v0 = x0[W:, 3:6].clone()
+    d = torch.from_numpy(np.random.default_rng(7).normal(size=tuple(v0.shape))).to(dev)
+
+    def loss(p, v):
+        x = torch.cat([x0[:W], torch.cat([x0[W:, :3], v, v, x0[W:, 9:]], 1)], 0)
+        com, _ = rollout(eng, x, law_from(p["kn"], p["zeta"], p["mu"]).to(dev), steps)
+        return ((com - target) ** 2).mean()
+
+    P = {k: torch.tensor(v, dtype=torch.float64, device=dev, requires_grad=True) for k, v in base.items()}
+    vv = v0.clone().requires_grad_(True)
+    loss(P, vv).backward()
+    an = {k: float(t.grad) for k, t in P.items()}
+    an["v0"] = float((vv.grad * d).sum())
+    out = {}
+    with torch.no_grad():
+        for k in ("kn", "zeta", "mu", "v0"):
+            h = 1e-6 * (base[k] if k != "v0" else 1.0)
+            vals = []
+            for sgn in (1, -1):
+                p = dict(base)
+                v = v0
+                if k == "v0":
+                    v = v0 + sgn * h * d
+                else:
+                    p[k] = base[k] + sgn * h
+                vals.append(float(loss(p, v)))
+            fd = (vals[0] - vals[1]) / (2 * h)
+            out[k] = {"adjoint": an[k], "fd": fd, "rel_err": abs(an[k] - fd) / abs(fd)}
+    return out
 
 
 def reference_arm(args):

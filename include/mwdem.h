@@ -40,7 +40,10 @@ enum {
     MWD_ST_PAIR_OVERFLOW = 8u,  /* broad phase produced more candidate pairs than the pair buffer holds */
     MWD_ST_CELL_RANGE = 16u,    /* a centre's cell key fell outside the scene's dense cell table */
     MWD_ST_CELL_CROWDED = 32u,  /* a cell held more members than the set-order emulation supports */
-    MWD_ST_BAD_SHAPE = 64u      /* a hull with more vertices than the staging capacity */
+    MWD_ST_BAD_SHAPE = 64u,     /* a hull with more vertices than the staging capacity */
+    MWD_ST_DEGENERATE_FACE = 128u, /* differentiable step: a logged contact face of zero area (skipped) */
+    MWD_ST_LOG_OVERFLOW = 256u,    /* differentiable step: more contacts than the topology log holds */
+    MWD_ST_FLY_RESET = 512u        /* differentiable step: a particle left the box and was stopped */
 };
 
 #define MWD_EPA_FACE_CAP 128   /* append-only EPA face list per pair */
@@ -208,6 +211,10 @@ typedef struct {
     int32_t n_verts;
     int32_t max_verts;       /* largest vertex count of any row (<= MWD_HULL_CAP) */
     int32_t pad;
+    const int32_t* vert_owner; /* optional (nv,) row of each vertex; with xform the integrator rewrites
+                                  the world vertices one thread per vertex (NULL: one block per 128 rows) */
+    float* xform;            /* optional (n,16) scratch: R(q_acc) row-major, then the centre as float
+                                hi + lo per axis */
 } mwd_state;
 
 typedef struct {
@@ -251,6 +258,8 @@ typedef struct {
     int32_t pad;
     int64_t total_cells;
     int64_t pair_cap;
+    int32_t* face_ids;     /* optional (pair_cap, 6): support-vertex indices (into each row's vertex table)
+                              of the final EPA face, A's three then B's, written where collision is 1 */
 } mwd_work;
 
 /* Scratch ints the device-wide scans need for arrays of n elements. */
@@ -278,6 +287,82 @@ int mwd_step(mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes
  * 8 x SM-count blocks of 256 threads, times it with CUDA events (synchronises the stream) and
  * writes the rate in TFLOP/s.  scratch: >= 8 x SM-count floats.  The narrow phase's roofline. */
 int mwd_probe_fp32(int32_t iters, float* scratch, double* tflops_out /* host */, mwd_stream_t stream);
+
+/* ------------------------------------------------------------------ differentiable step
+ *
+ * No reference counterpart: the reference has no gradients.  A single-scene FP64 restatement of
+ * the device step whose contact topology -- the pairs in contact and, per pair, the support
+ * vertices of the final EPA face -- is detected by the FP32 broad + narrow phase above and logged
+ * per step.  Given that topology, depth, normal and contact points are smooth functions of the two
+ * bodies' centres and vertex orientations (q_acc), so the step (contact force with zero tangential
+ * history, as the reference wipes it every step, MWDiem.py:966, then the leapfrog of
+ * gpu_Verlet.cu:164-323) is differentiable, and mwd_diff_adjoint applies its transpose.
+ *
+ * FP64 state row (32 doubles): centre 0-2, v 3-5, v_half 6-8, w_half_bf 9-11, w_bf 12-14, w 15-17,
+ * q 18-21, q_half 22-25, q_acc 26-29, unused 30-31; quaternions (w, x, y, z). */
+#define MWD_DIFF_ROW 32
+
+typedef struct {
+    int32_t A, B;        /* rows */
+    int32_t fa[3], fb[3]; /* final EPA face: support-vertex indices into A's and B's vertex tables */
+} mwd_contact_rec;
+
+typedef struct {
+    int32_t n;              /* rows, walls included (info bit 0) */
+    int32_t n_particles;    /* non-wall rows: the centre-of-mass average */
+    int32_t n_steps;        /* capacity of step_off / step_count / com (steps of one forward) */
+    int32_t ckpt_every;     /* checkpoint interval K: ckpt[k] holds the state after step k K */
+    int32_t contact_point;  /* 0: the reference's (cpA - cpB) / 2 (gpu_fine_contact_detection.cu:677), whose
+                               torque arm is about minus the centre's position vector; 1: the midpoint
+                               (cpA + cpB) / 2 */
+    int32_t pad;
+    double dt;
+    double box[6];          /* fly-away box x_max, x_min, y_max, y_min, z_max, z_min */
+    const double* inertia;  /* (n,4) Ix, Iy, Iz, inertia size (the contact law's I) */
+    const double* inv_inertia; /* (n,4) 1/Ix, 1/Iy, 1/Iz, 1/m */
+    const double* ext;      /* (n,4) external force (gravity) */
+    const float* body_verts; /* CSR body-frame vertices (float4), as in mwd_state */
+    const int32_t* vert_off;
+    const int32_t* info;
+    const double* law;      /* (8,) Kn, en, et, mu of particle pairs, then of wall pairs */
+    double* F;              /* (n,4) contact force accumulator, zero between steps */
+    double* T;              /* (n,4) contact torque accumulator, zero between steps */
+    mwd_contact_rec* rec;   /* topology log */
+    int64_t rec_cap;
+    int64_t* step_off;      /* (n_steps + 1,) first record of each step; step_off[0] = 0 */
+    int32_t* step_count;    /* (n_steps,) records of each step; zero before a forward */
+    int32_t* t_dev;         /* (1,) device step counter (steps of a captured forward read it) */
+    uint32_t* sync;         /* (1,) zero: block counter of the integrator's step advance */
+    double* com;            /* optional (n_steps, 4): centre of mass of the particle rows after each step */
+    double* ckpt;           /* optional (n_steps / ckpt_every + 1, n, 32) */
+    uint32_t* status;       /* (1,) status word (MWD_ST_*) */
+} mwd_diff;
+
+/* Log the contacts of the narrow phase just run (work->collision == 1, work->face_ids) as step
+ * *d->t_dev of the topology log.  work->collision and work->face_ids must be set. */
+int mwd_diff_collect(const mwd_diff* d, const mwd_work* work, mwd_stream_t stream);
+
+/* Contact force and torque of step t (t < 0: *d->t_dev) from the logged topology and the FP64
+ * state x, added to d->F, d->T. */
+int mwd_diff_force(const mwd_diff* d, const double* x, int32_t t, mwd_stream_t stream);
+
+/* Integrator of step t (t < 0: *d->t_dev, and the counter advances) from x with d->F + ext and
+ * d->T into x_out (may alias x); zeroes d->F, d->T.  Optional: FT_store (n,8) receives the total
+ * force and torque used; mirror (not NULL) receives the FP32 copies the detection reads (pos,
+ * vel, w, q, q_acc, world_verts; force/torque zeroed); with t < 0 also com[t] and the checkpoint. */
+int mwd_diff_integrate(const mwd_diff* d, const double* x, double* x_out, double* FT_store, mwd_state* mirror,
+                       int32_t t, mwd_stream_t stream);
+
+/* FP32 copies of the FP64 state x into mirror (pos, vel, w, q, q_acc, world_verts). */
+int mwd_diff_mirror(const mwd_diff* d, const double* x, mwd_state* mirror, mwd_stream_t stream);
+
+/* Transpose of step t: lam is the gradient with respect to the state after the step; com_grad
+ * (optional, (n_steps,4)) the gradient with respect to com[t].  Writes the gradient with respect
+ * to the state before the step into lam_prev (overwritten; must not alias lam) and adds the law's
+ * gradient to glaw (8,).  x: state before the step; FT: the force/torque of the step (FT_store of
+ * mwd_diff_integrate); gFT: (n,8) scratch. */
+int mwd_diff_adjoint(const mwd_diff* d, const double* x, const double* FT, int32_t t, const double* lam,
+                     double* lam_prev, const double* com_grad, double* gFT, double* glaw, mwd_stream_t stream);
 
 /* Library information. */
 const char* mwd_last_error(void);

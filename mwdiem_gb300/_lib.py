@@ -24,6 +24,9 @@ ST_PAIR_OVERFLOW = 8
 ST_CELL_RANGE = 16
 ST_CELL_CROWDED = 32
 ST_BAD_SHAPE = 64
+ST_DEGENERATE_FACE = 128
+ST_LOG_OVERFLOW = 256
+ST_FLY_RESET = 512
 
 EPA_FACE_CAP = 128
 EPA_VERT_CAP = 32
@@ -33,7 +36,8 @@ NOALLOC_MAX_PAIRS = 1 << 18
 
 STATUS_NAMES = {ST_EPA_NOCONV: "EPA_NOCONV", ST_EPA_OVERFLOW: "EPA_OVERFLOW", ST_GJK_NOCONV: "GJK_NOCONV",
                 ST_PAIR_OVERFLOW: "PAIR_OVERFLOW", ST_CELL_RANGE: "CELL_RANGE", ST_CELL_CROWDED: "CELL_CROWDED",
-                ST_BAD_SHAPE: "BAD_SHAPE"}
+                ST_BAD_SHAPE: "BAD_SHAPE", ST_DEGENERATE_FACE: "DEGENERATE_FACE", ST_LOG_OVERFLOW: "LOG_OVERFLOW",
+                ST_FLY_RESET: "FLY_RESET"}
 
 
 class MwdError(RuntimeError):
@@ -67,7 +71,8 @@ class State(C.Structure):
     _fields_ = [(n, _P) for n in ("pos", "dx_all", "vel", "vel_half", "w_half_bf", "w_bf", "w", "q", "q_half",
                                   "q_all", "q_acc", "force", "torque", "ext_force", "ext_torque", "inertia",
                                   "inv_inertia", "info", "wall_normal", "vert_off", "body_verts", "world_verts")] + \
-               [("n", C.c_int32), ("n_verts", C.c_int32), ("max_verts", C.c_int32), ("pad", C.c_int32)]
+               [("n", C.c_int32), ("n_verts", C.c_int32), ("max_verts", C.c_int32), ("pad", C.c_int32),
+                ("vert_owner", _P), ("xform", _P)]
 
 
 class Scene(C.Structure):
@@ -83,7 +88,27 @@ class Work(C.Structure):
                [("crowded_cap", C.c_int64), ("work_counters", _P), ("epa_count", _P), ("epa_rec", _P),
                 ("epa_cap", C.c_int64), ("sorted_pos", _P), ("sorted_cell", _P), ("cull_pairs", C.c_int32),
                 ("pad", C.c_int32), ("total_cells", C.c_int64),
-                ("pair_cap", C.c_int64)]
+                ("pair_cap", C.c_int64), ("face_ids", _P)]
+
+
+DIFF_ROW = 32
+# FP64 state row of the differentiable step (include/mwdem.h): slices by name
+DIFF_SLICES = {"c": slice(0, 3), "v": slice(3, 6), "v_half": slice(6, 9), "w_half_bf": slice(9, 12),
+               "w_bf": slice(12, 15), "w": slice(15, 18), "q": slice(18, 22), "q_half": slice(22, 26),
+               "q_acc": slice(26, 30)}
+
+
+class ContactRec(C.Structure):
+    _fields_ = [("A", C.c_int32), ("B", C.c_int32), ("fa", C.c_int32 * 3), ("fb", C.c_int32 * 3)]
+
+
+class Diff(C.Structure):
+    _fields_ = [("n", C.c_int32), ("n_particles", C.c_int32), ("n_steps", C.c_int32), ("ckpt_every", C.c_int32),
+                ("contact_point", C.c_int32), ("pad", C.c_int32), ("dt", C.c_double), ("box", C.c_double * 6)] + \
+               [(n, _P) for n in ("inertia", "inv_inertia", "ext", "body_verts", "vert_off", "info", "law", "F", "T",
+                                  "rec")] + \
+               [("rec_cap", C.c_int64)] + \
+               [(n, _P) for n in ("step_off", "step_count", "t_dev", "sync", "com", "ckpt", "status")]
 
 
 _lock = threading.Lock()
@@ -119,6 +144,11 @@ def lib():
             "mwd_probe_fp32": (C.c_int, [i32, _P, C.POINTER(C.c_double), _P]),
             "mwd_contact_pairs_noalloc": (C.c_int, [i64, i32, i32] + [_P] * 20 +
                                           [C.POINTER(ContactParams), _P, _P, _P]),
+            "mwd_diff_collect": (C.c_int, [C.POINTER(Diff), C.POINTER(Work), _P]),
+            "mwd_diff_force": (C.c_int, [C.POINTER(Diff), _P, i32, _P]),
+            "mwd_diff_integrate": (C.c_int, [C.POINTER(Diff), _P, _P, _P, C.POINTER(State), i32, _P]),
+            "mwd_diff_mirror": (C.c_int, [C.POINTER(Diff), _P, C.POINTER(State), _P]),
+            "mwd_diff_adjoint": (C.c_int, [C.POINTER(Diff), _P, _P, i32, _P, _P, _P, _P, _P, _P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(h, name)
@@ -131,7 +161,8 @@ def lib():
 EXPORTED = ("mwd_last_error", "mwd_version", "mwd_num_sms", "mwd_scan_tmp_ints", "mwd_derive_material",
             "mwd_contact_pairs", "mwd_verlet_ref", "mwd_cell_keys", "mwd_wall_pairs", "mwd_linked_cell_hash",
             "mwd_broadphase", "mwd_narrow_force", "mwd_integrate", "mwd_step", "mwd_probe_fp32",
-            "mwd_contact_pairs_noalloc")
+            "mwd_contact_pairs_noalloc", "mwd_diff_collect", "mwd_diff_force", "mwd_diff_integrate",
+            "mwd_diff_mirror", "mwd_diff_adjoint")
 
 
 def check(rc: int):

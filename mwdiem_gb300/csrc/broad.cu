@@ -14,7 +14,11 @@
 //   scan     exclusive scan of the counts = output offsets
 //   emit     the same walk, writing [A, B] pairs
 //
-// Every step is deterministic: the pair list depends only on the inputs.
+// The list of (count, scan, emit) depends only on the inputs and is in cell order.  The device
+// step's broad phase (append mode) replaces those three stages by one kernel: each thread walks its
+// row twice (count, then write) and a warp reserves its slots with one atomic, so the same oriented
+// pairs come out in an order that varies from run to run (the orientation, A before B, still comes
+// from the set order).
 #include "broad.cuh"
 #include "common.cuh"
 
@@ -202,6 +206,7 @@ __device__ __forceinline__ int64_t row_key(const BroadArgs& a, const mwd_scene& 
 
 __global__ void assign_kernel(BroadArgs a)
 {
+    if (a.append && blockIdx.x == 0 && threadIdx.x == 0) *a.n_pairs = 0;  // appended to by pairs_append_kernel
     const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= a.row_hi) return;
     if (is_wall(a, r)) {
@@ -317,25 +322,11 @@ __global__ void __launch_bounds__(32) order_crowded_kernel(BroadArgs a)
     }
 }
 
-template <bool EMIT>
-__global__ void pairs_kernel(BroadArgs a)
+// every candidate of the row at sorted position t (row r, cell g), passed to sink(A, B)
+template <class Sink>
+__device__ __forceinline__ void walk_pairs(const BroadArgs& a, int t, int r, int g, const mwd_scene& sc, Sink&& sink)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!EMIT && t == 0) *a.n_crowded = 0;  // consumed by the crowded-cell pass, which ran before
-    const int n_sorted = a.cell_start[a.total_cells];
-    if (t >= n_sorted) {
-        if (!EMIT && t < a.row_hi - a.row_lo) a.pair_count[t] = 0;
-        return;
-    }
-    const int r = a.sorted[t];
     const bool cull = a.cull && a.sorted_pos;
-    const int g = a.sorted_cell ? a.sorted_cell[t] : a.cell_of[r];
-    const mwd_scene& sc = a.scenes[scene_of(a, r)];
-    int c = 0;
-    int64_t out = 0;
-    int32_t* pairs = a.pairs;
-    const int64_t cap = a.pair_cap;
-    if (EMIT) out = a.pair_count[t];
     const float4 me = cull ? a.sorted_pos[t] : make_float4(0.f, 0.f, 0.f, 0.f);
     // B at sorted position j (-1: a wall row given by B alone)
     auto put = [&](int A, int B, int j) {
@@ -349,12 +340,7 @@ __global__ void pairs_kernel(BroadArgs a)
             }
             if (spheres_apart_f(me, pb)) return;
         }
-        if (EMIT) {
-            if (out < cap) reinterpret_cast<int2*>(pairs)[out] = make_int2(A, B);
-            ++out;
-        } else {
-            ++c;
-        }
+        sink(A, B);
     };
     // wall candidates (MWDiem.py:808-811): pair [particle, wall]
     if (a.walls) {
@@ -367,9 +353,8 @@ __global__ void pairs_kernel(BroadArgs a)
         }
     }
     // later members of the same cell, in set order
-    const int cs = a.cell_start[g], ce = a.cell_start[g + 1];
+    const int ce = a.cell_start[g + 1];
     for (int j = t + 1; j < ce; ++j) put(r, a.sorted[j], j);
-    (void)cs;
     // forward neighbours
     const int64_t local = (int64_t)g - sc.cell_base;
     const int64_t nx = sc.nx, nxy = sc.nx * sc.ny;
@@ -388,7 +373,71 @@ __global__ void pairs_kernel(BroadArgs a)
 #pragma unroll
     for (int o = 0; o < 7; ++o)
         for (int j = rs[o]; j < re[o]; ++j) put(r, a.sorted[j], j);
-    if (!EMIT) a.pair_count[t] = c;
+}
+
+template <bool EMIT>
+__global__ void pairs_kernel(BroadArgs a)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!EMIT && t == 0) *a.n_crowded = 0;  // consumed by the crowded-cell pass, which ran before
+    const int n_sorted = a.cell_start[a.total_cells];
+    if (t >= n_sorted) {
+        if (!EMIT && t < a.row_hi - a.row_lo) a.pair_count[t] = 0;
+        return;
+    }
+    const int r = a.sorted[t];
+    const int g = a.sorted_cell ? a.sorted_cell[t] : a.cell_of[r];
+    const mwd_scene& sc = a.scenes[scene_of(a, r)];
+    if (EMIT) {
+        int64_t out = a.pair_count[t];
+        const int64_t cap = a.pair_cap;
+        int2* pairs = reinterpret_cast<int2*>(a.pairs);
+        walk_pairs(a, t, r, g, sc, [&](int A, int B) {
+            if (out < cap) pairs[out] = make_int2(A, B);
+            ++out;
+        });
+    } else {
+        int c = 0;
+        walk_pairs(a, t, r, g, sc, [&](int, int) { ++c; });
+        a.pair_count[t] = c;
+    }
+}
+
+// count, reserve (one atomic per warp on n_pairs, zeroed by assign_kernel), write
+__global__ void __launch_bounds__(256) pairs_append_kernel(BroadArgs a)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) *a.n_crowded = 0;  // consumed by the crowded-cell pass, which ran before
+    const int n_sorted = a.cell_start[a.total_cells];
+    const bool live = t < n_sorted;
+    int r = 0, g = 0, c = 0;
+    const mwd_scene* sc = nullptr;
+    if (live) {
+        r = a.sorted[t];
+        g = a.sorted_cell ? a.sorted_cell[t] : a.cell_of[r];
+        sc = &a.scenes[scene_of(a, r)];
+        walk_pairs(a, t, r, g, *sc, [&](int, int) { ++c; });
+    }
+    const int lane = threadIdx.x & 31;
+    int inc = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, inc, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(reinterpret_cast<unsigned long long*>(a.n_pairs), (unsigned long long)total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    if (!live || c == 0) return;
+    int64_t out = (int64_t)base + inc - c;
+    const int64_t cap = a.pair_cap;
+    if (out + c > cap) set_status(a.status, MWD_ST_PAIR_OVERFLOW);
+    int2* pairs = reinterpret_cast<int2*>(a.pairs);
+    walk_pairs(a, t, r, g, *sc, [&](int A, int B) {
+        if (out < cap) pairs[out] = make_int2(A, B);
+        ++out;
+    });
 }
 
 // wall-major candidates for the reference-layout entry point (MWDiem.py:808-811)
@@ -482,6 +531,11 @@ int launch_broad(const BroadArgs& a, cudaStream_t s)
     order_kernel<<<blocks(rows, T), T, 0, s>>>(a);
     order_crowded_kernel<<<(unsigned)(a.crowded_cap < 1024 ? (a.crowded_cap > 0 ? a.crowded_cap : 1) : 1024), 32, 0, s>>>(a);
     // rows that have a cell are at most `rows`; threads past cell_start[total] exit
+    if (a.append) {
+        pairs_append_kernel<<<blocks(rows, T), T, 0, s>>>(a);
+        MWD_CUDA(cudaGetLastError());
+        return MWD_OK;
+    }
     pairs_kernel<false><<<blocks(rows, T), T, 0, s>>>(a);
     rc = launch_scan(a.pair_count, rows, a.pair_count, a.scan_tmp, a.n_pairs, a.pair_cap, a.status,
                      MWD_ST_PAIR_OVERFLOW, s);

@@ -14,6 +14,9 @@ struct BroadArgs {
     const mwd_scene* scenes;     // device scene table
     int32_t walls;               // 1: emit wall candidates
     int32_t cull;                // 1: drop pairs whose bounding spheres are apart (pos.w = radius)
+    int32_t append;              // 1: one kernel appends pairs (one atomic per warp, list order varies);
+                                 // 0: count, scan, emit (list in cell order)
+    int32_t pad_;
     int32_t* cell_count;         // (total_cells,) zero on entry and on exit
     int32_t* cell_start;         // (total_cells+1,)
     int32_t* cell_of;            // (n,)

@@ -395,6 +395,7 @@ int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_s
     a.total_cells = work->total_cells;
     a.pair_cap = work->pair_cap;
     a.cull = work->cull_pairs ? 1 : 0;
+    a.append = 1;
     a.sorted_pos = reinterpret_cast<float4*>(work->sorted_pos);
     a.sorted_cell = work->sorted_cell;
     return launch_broad(a, reinterpret_cast<cudaStream_t>(stream));
@@ -425,6 +426,7 @@ int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work*
     a.status = work->status;
     a.work_counters = reinterpret_cast<unsigned long long*>(work->work_counters);
     a.hull_cap = st->max_verts;
+    a.face_ids = work->face_ids;
     if (work->epa_rec && work->epa_count && work->epa_cap > 0) {
         a.epa_count = work->epa_count;
         a.epa_rec = work->epa_rec;

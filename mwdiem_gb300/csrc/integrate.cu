@@ -220,6 +220,106 @@ __device__ __forceinline__ float4 rot_increment(f3 w, float s)
     return make_float4(cs, h.x, h.y, h.z);
 }
 
+// one row's update (walls: unchanged); returns the centre and q_acc the vertex pass uses
+__device__ __forceinline__ void row_update(const mwd_state& st, const mwd_scene* __restrict__ scenes, int P,
+                                           dpos& pos_out, float4& qacc_out)
+{
+    const int info = st.info[P];
+    dpos pos = reinterpret_cast<const dpos*>(st.pos)[P];
+    float4 qacc = ld4(st.q_acc, P);
+    if (!(info & 1)) {
+        const mwd_scene& sc = scenes[info >> 1];
+        const float dt = (float)sc.dt;
+        float4 Fa = ld4(st.force, P), Ta = ld4(st.torque, P);
+        float4 Fe = ld4(st.ext_force, P), Te = ld4(st.ext_torque, P);
+        f3 F = mk3(Fa.x + Fe.x, Fa.y + Fe.y, Fa.z + Fe.z);
+        f3 T = mk3(Ta.x + Te.x, Ta.y + Te.y, Ta.z + Te.z);
+        float4 I = ld4(st.inertia, P), Ii = ld4(st.inv_inertia, P);
+        const float invm = Ii.w;
+        f3 vh = xyz(ld4(st.vel_half, P));
+        f3 whbf = xyz(ld4(st.w_half_bf, P));
+        f3 wbf = xyz(ld4(st.w_bf, P));
+        f3 w = xyz(ld4(st.w, P));
+        float4 q = ld4(st.q, P), qh = ld4(st.q_half, P), qall = ld4(st.q_all, P);
+        dpos dxall = reinterpret_cast<const dpos*>(st.dx_all)[P];
+
+        f3 v32 = vh + F * (invm * dt);
+        f3 tbf = qtrip(qconj(q), T, q);
+        f3 p1 = mk3(I.x * wbf.x, I.y * wbf.y, I.z * wbf.z);
+        f3 p2 = tbf - cross(wbf, p1);
+        f3 alpha = mk3(Ii.x * p2.x, Ii.y * p2.y, Ii.z * p2.z);
+        f3 w32bf = whbf + alpha * dt;
+        float4 q32 = qmul(rot_increment(w, dt * 0.5f), qh);
+        vh = v32;
+        qh = q32;
+        whbf = w32bf;
+        f3 dx = vh * dt;
+        dxall.x += (double)dx.x;
+        dxall.y += (double)dx.y;
+        dxall.z += (double)dx.z;
+        f3 w34bf = whbf + alpha * (dt * 0.25f);
+        f3 w34 = qtrip(qh, w34bf, qconj(qh));
+        float4 qold = q;
+        q = qmul(rot_increment(w34, dt * 0.25f), qh);
+        qall = qmul(q, qold);
+        wbf = whbf + alpha * (dt * 0.5f);
+        w = qtrip(q, wbf, qconj(q));
+        f3 v = vh + F * (invm * dt);
+        // vertices compound the rotation q every step (gpu_Verlet.cu:279-305): q_acc <- q q_acc
+        qacc = qmul(q, qacc);
+        float qn = rsqrtf(qacc.x * qacc.x + qacc.y * qacc.y + qacc.z * qacc.z + qacc.w * qacc.w);
+        qacc = make_float4(qacc.x * qn, qacc.y * qn, qacc.z * qn, qacc.w * qn);
+        dpos np;
+        np.x = pos.x + (double)dx.x;
+        np.y = pos.y + (double)dx.y;
+        np.z = pos.z + (double)dx.z;
+        np.w = pos.w;
+        if (np.x > sc.box[0] || np.x < sc.box[1] || np.y > sc.box[2] || np.y < sc.box[3] || np.z > sc.box[4] ||
+            np.z < sc.box[5]) {
+            // fly-away reset (gpu_Verlet.cu:338-352): stop the particle, undo the move
+            v = vh = whbf = wbf = w = mk3(0.f, 0.f, 0.f);
+            np = pos;
+        }
+        pos = np;
+        reinterpret_cast<dpos*>(st.pos)[P] = pos;
+        reinterpret_cast<dpos*>(st.dx_all)[P] = dxall;
+        st4(st.vel, P, f4(v, 0.f));
+        st4(st.vel_half, P, f4(vh, 0.f));
+        st4(st.w_half_bf, P, f4(whbf, 0.f));
+        st4(st.w_bf, P, f4(wbf, 0.f));
+        st4(st.w, P, f4(w, 0.f));
+        st4(st.q, P, q);
+        st4(st.q_half, P, qh);
+        st4(st.q_all, P, qall);
+        st4(st.q_acc, P, qacc);
+        st4(st.force, P, make_float4(0.f, 0.f, 0.f, 0.f));
+        st4(st.torque, P, make_float4(0.f, 0.f, 0.f, 0.f));
+    }
+    pos_out = pos;
+    qacc_out = qacc;
+}
+
+// R(q_acc) row-major and the centre as hi + lo floats per axis
+__device__ __forceinline__ void row_xform(float4 qacc, dpos pos, float* R, float* c)
+{
+    const float qw = qacc.x, qx = qacc.y, qy = qacc.z, qz = qacc.w;
+    R[0] = 1.f - 2.f * (qy * qy + qz * qz); R[1] = 2.f * (qx * qy - qw * qz); R[2] = 2.f * (qx * qz + qw * qy);
+    R[3] = 2.f * (qx * qy + qw * qz); R[4] = 1.f - 2.f * (qx * qx + qz * qz); R[5] = 2.f * (qy * qz - qw * qx);
+    R[6] = 2.f * (qx * qz - qw * qy); R[7] = 2.f * (qy * qz + qw * qx); R[8] = 1.f - 2.f * (qx * qx + qy * qy);
+    const float hx = (float)pos.x, hy = (float)pos.y, hz = (float)pos.z;
+    c[0] = hx; c[1] = (float)(pos.x - (double)hx);
+    c[2] = hy; c[3] = (float)(pos.y - (double)hy);
+    c[4] = hz; c[5] = (float)(pos.z - (double)hz);
+}
+
+__device__ __forceinline__ float4 world_vertex(const float* R, const float* c, float4 r0)
+{
+    const float rx = R[0] * r0.x + R[1] * r0.y + R[2] * r0.z;
+    const float ry = R[3] * r0.x + R[4] * r0.y + R[5] * r0.z;
+    const float rz = R[6] * r0.x + R[7] * r0.y + R[8] * r0.z;
+    return make_float4(c[0] + (rx + c[1]), c[2] + (ry + c[3]), c[4] + (rz + c[5]), 0.f);
+}
+
 __global__ void __launch_bounds__(RB) integrate_kernel(mwd_state st, const mwd_scene* __restrict__ scenes,
                                                        uint32_t* status)
 {
@@ -230,87 +330,10 @@ __global__ void __launch_bounds__(RB) integrate_kernel(mwd_state st, const mwd_s
     const int p0 = blockIdx.x * RB;
     const int rows = min(RB, st.n - p0);
     if (P < st.n) {
-        const int info = st.info[P];
-        dpos pos = reinterpret_cast<const dpos*>(st.pos)[P];
-        float4 qacc = ld4(st.q_acc, P);
-        if (!(info & 1)) {
-            const mwd_scene& sc = scenes[info >> 1];
-            const float dt = (float)sc.dt;
-            float4 Fa = ld4(st.force, P), Ta = ld4(st.torque, P);
-            float4 Fe = ld4(st.ext_force, P), Te = ld4(st.ext_torque, P);
-            f3 F = mk3(Fa.x + Fe.x, Fa.y + Fe.y, Fa.z + Fe.z);
-            f3 T = mk3(Ta.x + Te.x, Ta.y + Te.y, Ta.z + Te.z);
-            float4 I = ld4(st.inertia, P), Ii = ld4(st.inv_inertia, P);
-            const float invm = Ii.w;
-            f3 vh = xyz(ld4(st.vel_half, P));
-            f3 whbf = xyz(ld4(st.w_half_bf, P));
-            f3 wbf = xyz(ld4(st.w_bf, P));
-            f3 w = xyz(ld4(st.w, P));
-            float4 q = ld4(st.q, P), qh = ld4(st.q_half, P), qall = ld4(st.q_all, P);
-            dpos dxall = reinterpret_cast<const dpos*>(st.dx_all)[P];
-
-            f3 v32 = vh + F * (invm * dt);
-            f3 tbf = qtrip(qconj(q), T, q);
-            f3 p1 = mk3(I.x * wbf.x, I.y * wbf.y, I.z * wbf.z);
-            f3 p2 = tbf - cross(wbf, p1);
-            f3 alpha = mk3(Ii.x * p2.x, Ii.y * p2.y, Ii.z * p2.z);
-            f3 w32bf = whbf + alpha * dt;
-            float4 q32 = qmul(rot_increment(w, dt * 0.5f), qh);
-            vh = v32;
-            qh = q32;
-            whbf = w32bf;
-            f3 dx = vh * dt;
-            dxall.x += (double)dx.x;
-            dxall.y += (double)dx.y;
-            dxall.z += (double)dx.z;
-            f3 w34bf = whbf + alpha * (dt * 0.25f);
-            f3 w34 = qtrip(qh, w34bf, qconj(qh));
-            float4 qold = q;
-            q = qmul(rot_increment(w34, dt * 0.25f), qh);
-            qall = qmul(q, qold);
-            wbf = whbf + alpha * (dt * 0.5f);
-            w = qtrip(q, wbf, qconj(q));
-            f3 v = vh + F * (invm * dt);
-            // vertices compound the rotation q every step (gpu_Verlet.cu:279-305): q_acc <- q q_acc
-            qacc = qmul(q, qacc);
-            float qn = rsqrtf(qacc.x * qacc.x + qacc.y * qacc.y + qacc.z * qacc.z + qacc.w * qacc.w);
-            qacc = make_float4(qacc.x * qn, qacc.y * qn, qacc.z * qn, qacc.w * qn);
-            dpos np;
-            np.x = pos.x + (double)dx.x;
-            np.y = pos.y + (double)dx.y;
-            np.z = pos.z + (double)dx.z;
-            np.w = pos.w;
-            if (np.x > sc.box[0] || np.x < sc.box[1] || np.y > sc.box[2] || np.y < sc.box[3] || np.z > sc.box[4] ||
-                np.z < sc.box[5]) {
-                // fly-away reset (gpu_Verlet.cu:338-352): stop the particle, undo the move
-                v = vh = whbf = wbf = w = mk3(0.f, 0.f, 0.f);
-                np = pos;
-            }
-            pos = np;
-            reinterpret_cast<dpos*>(st.pos)[P] = pos;
-            reinterpret_cast<dpos*>(st.dx_all)[P] = dxall;
-            st4(st.vel, P, f4(v, 0.f));
-            st4(st.vel_half, P, f4(vh, 0.f));
-            st4(st.w_half_bf, P, f4(whbf, 0.f));
-            st4(st.w_bf, P, f4(wbf, 0.f));
-            st4(st.w, P, f4(w, 0.f));
-            st4(st.q, P, q);
-            st4(st.q_half, P, qh);
-            st4(st.q_all, P, qall);
-            st4(st.q_acc, P, qacc);
-            st4(st.force, P, make_float4(0.f, 0.f, 0.f, 0.f));
-            st4(st.torque, P, make_float4(0.f, 0.f, 0.f, 0.f));
-        }
-        // rotation matrix of q_acc and the centre as hi + lo floats, for the vertex pass
-        const float qw = qacc.x, qx = qacc.y, qy = qacc.z, qz = qacc.w;
-        float* R = s_R[threadIdx.x];
-        R[0] = 1.f - 2.f * (qy * qy + qz * qz); R[1] = 2.f * (qx * qy - qw * qz); R[2] = 2.f * (qx * qz + qw * qy);
-        R[3] = 2.f * (qx * qy + qw * qz); R[4] = 1.f - 2.f * (qx * qx + qz * qz); R[5] = 2.f * (qy * qz - qw * qx);
-        R[6] = 2.f * (qx * qz - qw * qy); R[7] = 2.f * (qy * qz + qw * qx); R[8] = 1.f - 2.f * (qx * qx + qy * qy);
-        float hx = (float)pos.x, hy = (float)pos.y, hz = (float)pos.z;
-        s_c[threadIdx.x][0] = hx; s_c[threadIdx.x][1] = (float)(pos.x - (double)hx);
-        s_c[threadIdx.x][2] = hy; s_c[threadIdx.x][3] = (float)(pos.y - (double)hy);
-        s_c[threadIdx.x][4] = hz; s_c[threadIdx.x][5] = (float)(pos.z - (double)hz);
+        dpos pos;
+        float4 qacc;
+        row_update(st, scenes, P, pos, qacc);
+        row_xform(qacc, pos, s_R[threadIdx.x], s_c[threadIdx.x]);
         s_off[threadIdx.x] = st.vert_off[P];
     }
     if (threadIdx.x == 0) s_off[rows] = st.vert_off[p0 + rows];
@@ -336,16 +359,43 @@ __global__ void __launch_bounds__(RB) integrate_kernel(mwd_state st, const mwd_s
                 int mid = (lo + hi + 1) >> 1;
                 if (s_off[mid] <= j) lo = mid; else hi = mid - 1;
             }
-            const float* R = s_R[lo];
-            const float* c = s_c[lo];
-            float rx = R[0] * r0[k].x + R[1] * r0[k].y + R[2] * r0[k].z;
-            float ry = R[3] * r0[k].x + R[4] * r0[k].y + R[5] * r0[k].z;
-            float rz = R[6] * r0[k].x + R[7] * r0[k].y + R[8] * r0[k].z;
-            wv[j] = make_float4(c[0] + (rx + c[1]), c[2] + (ry + c[3]), c[4] + (rz + c[5]), 0.f);
+            wv[j] = world_vertex(s_R[lo], s_c[lo], r0[k]);
         }
     }
 }
 
+// the row pass of the split integrator: one thread per row, the transform to st.xform
+__global__ void __launch_bounds__(RB) integrate_rows_kernel(mwd_state st, const mwd_scene* __restrict__ scenes,
+                                                            uint32_t* status)
+{
+    const int P = blockIdx.x * RB + threadIdx.x;
+    if (P >= st.n) return;
+    dpos pos;
+    float4 qacc;
+    row_update(st, scenes, P, pos, qacc);
+    float x[16];
+    row_xform(qacc, pos, x, x + 9);
+    x[15] = 0.f;
+    float4* o = reinterpret_cast<float4*>(st.xform) + 4 * (size_t)P;
+    o[0] = make_float4(x[0], x[1], x[2], x[3]);
+    o[1] = make_float4(x[4], x[5], x[6], x[7]);
+    o[2] = make_float4(x[8], x[9], x[10], x[11]);
+    o[3] = make_float4(x[12], x[13], x[14], x[15]);
+}
+
+// the vertex pass of the split integrator: one thread per vertex
+__global__ void __launch_bounds__(256) world_verts_kernel(mwd_state st)
+{
+    const int j = blockIdx.x * 256 + threadIdx.x;
+    if (j >= st.n_verts) return;
+    const int o = st.vert_owner[j];
+    const float4* xf = reinterpret_cast<const float4*>(st.xform) + 4 * (size_t)o;
+    const float4 a = xf[0], b = xf[1], c = xf[2], d = xf[3];
+    const float R[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
+    const float cc[6] = {c.y, c.z, c.w, d.x, d.y, d.z};
+    const float4 r0 = __ldg(reinterpret_cast<const float4*>(st.body_verts) + j);
+    reinterpret_cast<float4*>(st.world_verts)[j] = world_vertex(R, cc, r0);
+}
 }  // namespace
 
 int launch_verlet_ref(const VerletRefArgs& a, cudaStream_t s)
@@ -359,7 +409,12 @@ int launch_verlet_ref(const VerletRefArgs& a, cudaStream_t s)
 int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, cudaStream_t s)
 {
     if (st.n <= 0) return MWD_OK;
-    integrate_kernel<<<(st.n + RB - 1) / RB, RB, 0, s>>>(st, scenes, status);
+    if (st.vert_owner && st.xform) {
+        integrate_rows_kernel<<<(st.n + RB - 1) / RB, RB, 0, s>>>(st, scenes, status);
+        if (st.n_verts > 0) world_verts_kernel<<<(st.n_verts + 255) / 256, 256, 0, s>>>(st);
+    } else {
+        integrate_kernel<<<(st.n + RB - 1) / RB, RB, 0, s>>>(st, scenes, status);
+    }
     MWD_CUDA(cudaGetLastError());
     return MWD_OK;
 }

@@ -226,6 +226,27 @@ def pour_scene(n=20000, seed=0, box=40.0, spacing=2.6, jitter=0.1, n_min=12, n_m
                      name=name)
 
 
+def packed_scene(n=16, seed=0, box=8.0, spacing=2.2, z0=1.0, jitter=0.05, vel=0.5, n_min=12, n_max=32,
+                 r_min=0.8, r_max=1.2, zeta=0.3, kn=1e5, mu=0.5, dt=5e-5, density=1.0, name="packed"):
+    """Random hulls on a lattice closer than their diameters (neighbours and the floor overlap from
+    the first step), random orientations and velocities: a small scene whose contacts are active
+    from step 0 (the differentiable step's finite-difference case)."""
+    rng = np.random.default_rng(seed)
+    en = restitution_from_damping(zeta)
+    centres, layers = lattice(n, box, box, spacing, jitter, rng, z0=z0)
+    height = float(z0 + layers * spacing + 4 * r_max)
+    walls = box_walls(box, box, height, 20 * r_max, density)
+    bodies = []
+    for _ in range(n):
+        b = fast_hull_body(rng, n_min, n_max, r_min, r_max, density)
+        q = shapes.random_quaternion(rng)
+        b.vertices = np.ascontiguousarray(b.vertices @ shapes.quat_to_matrix(q).T)
+        bodies.append(b)
+    v = rng.normal(size=(n, 3)) * vel
+    return SceneSpec(walls=walls, bodies=bodies, centres=centres, velocities=v, Kn=kn, en=en, et=en, mu=mu,
+                     Kn_wall=kn, en_wall=en, et_wall=en, mu_wall=mu, dt=dt, max_particlesize=2 * r_max, name=name)
+
+
 def settling_scene(seed=0, n_side=5, edge=1.0, spacing=1.5, jitter=0.1, zeta=0.3, kn=1e5, mu=0.5, dt=1e-4,
                    floor=10.0):
     """125 unit cubes (density 1) on a 5x5x5 lattice, random orientations, onto a 10 x 10 floor."""

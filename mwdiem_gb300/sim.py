@@ -161,6 +161,9 @@ class Simulator:
         I = cat["I"]
         inertia = np.concatenate([I, cat["size"][:, None]], 1)
         inv = np.concatenate([1.0 / I, 1.0 / cat["mass"][:, None]], 1)
+        # FP64 row constants and initial values (the differentiable step computes in FP64)
+        self.row_data = dict(inertia=inertia, inv_inertia=inv, ext=cat["ext"], pos=cat["pos"], vel=cat["vel"],
+                             info=cat["info"])
         z4 = torch.zeros((n, 4), **f32)
         t = {}
         t["pos"] = torch.from_numpy(pos).to(dev)
@@ -190,9 +193,12 @@ class Simulator:
         world = body.clone()
         world[:, :3] = (t["pos"][owner, :3] + body[:, :3].double()).float()
         t["world_verts"] = world
+        # the integrator's vertex pass: one thread per vertex, through each row's transform
+        t["vert_owner"] = owner.to(torch.int32)
+        t["xform"] = torch.zeros((n, 16), **f32)
         self.t = t
         st = State()
-        for k in _STATE_F64 + _STATE_F32 + ("info", "vert_off", "body_verts", "world_verts"):
+        for k in _STATE_F64 + _STATE_F32 + ("info", "vert_off", "body_verts", "world_verts", "vert_owner", "xform"):
             setattr(st, k, t[k].data_ptr())
         st.n = n
         st.n_verts = total

@@ -138,9 +138,10 @@ def test_two_pass_equals_single_pass():
     torch.cuda.synchronize()
     n = one.n_pairs()
     assert n == two.n_pairs()
-    c1 = one.w["collision"][:n].cpu().numpy()
-    c2 = two.w["collision"][:n].cpu().numpy()
-    assert np.array_equal(c1, c2) and (c1 == 1).sum() > 100
+    # the device step's pair list holds the same pairs in a run-dependent order: compare by pair
+    f1 = dict(zip(map(tuple, one.pairs().cpu().numpy().tolist()), one.w["collision"][:n].cpu().numpy().tolist()))
+    f2 = dict(zip(map(tuple, two.pairs().cpu().numpy().tolist()), two.w["collision"][:n].cpu().numpy().tolist()))
+    assert f1 == f2 and sum(v == 1 for v in f1.values()) > 100
     F1, F2 = one.t["force"].cpu().numpy(), two.t["force"].cpu().numpy()
     assert np.abs(F1 - F2).max() <= 1e-5 * np.abs(F1).max()
     T1, T2 = one.t["torque"].cpu().numpy(), two.t["torque"].cpu().numpy()
