@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--lanes", type=int, default=8)
+    ap.add_argument("--no-tune", action="store_true", help="use --lanes instead of the autotuner's choice")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-breakdown", action="store_true")
@@ -58,7 +59,9 @@ def parse():
                     help="differentiable calibration: 2,000 hulls, 5,000 steps, forward vs forward + adjoint")
     ap.add_argument("--calib-steps", type=int, default=5000)
     ap.add_argument("--calib-particles", type=int, default=2000)
-    ap.add_argument("--contact-point", default="reference", choices=["reference", "midpoint"])
+    ap.add_argument("--contact-point", default="midpoint", choices=["reference", "midpoint"],
+                    help="calibration's torque-arm contact point: the reference's (cpA - cpB)/2 spins particles "
+                         "far from the origin up until the 5,000-step pour flies apart, so the midpoint is the default")
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--batch-total", type=int, default=2_000_000)
     return ap.parse_args()
@@ -219,7 +222,7 @@ def main():
     V = sim.max_verts
     window = Window(sim, WINDOW_STEPS)
     from mwdiem_gb300 import autotune
-    tuning = autotune.tune_lanes(sim, steps=3)
+    tuning = {} if args.no_tune else autotune.tune_lanes(sim, steps=3)
     sim.capture(steps_per_replay=1)
     window.restore()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2

@@ -336,6 +336,8 @@ typedef struct {
     double* com;            /* optional (n_steps, 4): centre of mass of the particle rows after each step */
     double* ckpt;           /* optional (n_steps / ckpt_every + 1, n, 32) */
     uint32_t* status;       /* (1,) status word (MWD_ST_*) */
+    const int32_t* t_base;  /* optional (1,): an explicit step argument t >= 0 means step *t_base + t, so one
+                               captured segment of the backward replays at any checkpoint */
 } mwd_diff;
 
 /* Log the contacts of the narrow phase just run (work->collision == 1, work->face_ids) as step

@@ -108,7 +108,7 @@ class Diff(C.Structure):
                [(n, _P) for n in ("inertia", "inv_inertia", "ext", "body_verts", "vert_off", "info", "law", "F", "T",
                                   "rec")] + \
                [("rec_cap", C.c_int64)] + \
-               [(n, _P) for n in ("step_off", "step_count", "t_dev", "sync", "com", "ckpt", "status")]
+               [(n, _P) for n in ("step_off", "step_count", "t_dev", "sync", "com", "ckpt", "status", "t_base")]
 
 
 _lock = threading.Lock()

@@ -20,6 +20,7 @@
 // no per-pair tape is stored).  Everything is FP64.  The force kernel and the pair adjoint add into
 // per-row arrays with atomics; the law's gradient is reduced over a warp before its atomics.
 #include "common.cuh"
+#include "integrate.cuh"
 
 namespace mwd {
 namespace {
@@ -516,7 +517,11 @@ __device__ __forceinline__ void add4q(double* p, dq v)
     atomicAdd(p + 3, v.z);
 }
 
-__device__ __forceinline__ int step_of(const mwd_diff& d, int t) { return t >= 0 ? t : *d.t_dev; }
+// explicit steps are offset by *t_base when given; t < 0 reads the forward's device counter
+__device__ __forceinline__ int step_of(const mwd_diff& d, int t)
+{
+    return t >= 0 ? t + (d.t_base ? *d.t_base : 0) : *d.t_dev;
+}
 
 __device__ __forceinline__ void load_pair_in(const mwd_diff& d, const double* x, const mwd_contact_rec& rc, PairIn& p,
                                              bool& wall)
@@ -592,6 +597,27 @@ __device__ __forceinline__ void write_mirror(const mwd_state& m, int r, const do
     reinterpret_cast<float4*>(m.q_acc)[r] = make_float4((float)row[26], (float)row[27], (float)row[28], (float)row[29]);
     reinterpret_cast<float4*>(m.force)[r] = make_float4(0.f, 0.f, 0.f, 0.f);
     reinterpret_cast<float4*>(m.torque)[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (m.xform && m.vert_owner) {
+        // the row transform for the per-vertex pass (launch_world_verts): R(q_acc) from the float
+        // q_acc, as the device step forms it, and the centre as float hi + lo
+        const float qw = (float)row[26], qx = (float)row[27], qy = (float)row[28], qz = (float)row[29];
+        float x[16];
+        x[0] = 1.f - 2.f * (qy * qy + qz * qz); x[1] = 2.f * (qx * qy - qw * qz); x[2] = 2.f * (qx * qz + qw * qy);
+        x[3] = 2.f * (qx * qy + qw * qz); x[4] = 1.f - 2.f * (qx * qx + qz * qz); x[5] = 2.f * (qy * qz - qw * qx);
+        x[6] = 2.f * (qx * qz - qw * qy); x[7] = 2.f * (qy * qz + qw * qx); x[8] = 1.f - 2.f * (qx * qx + qy * qy);
+        for (int k = 0; k < 3; ++k) {
+            const float hi = (float)row[k];
+            x[9 + 2 * k] = hi;
+            x[10 + 2 * k] = (float)(row[k] - (double)hi);
+        }
+        x[15] = 0.f;
+        float4* o = reinterpret_cast<float4*>(m.xform) + 4 * (size_t)r;
+        o[0] = make_float4(x[0], x[1], x[2], x[3]);
+        o[1] = make_float4(x[4], x[5], x[6], x[7]);
+        o[2] = make_float4(x[8], x[9], x[10], x[11]);
+        o[3] = make_float4(x[12], x[13], x[14], x[15]);
+        return;
+    }
     const dq qa = ld4q(row + 26);
     const d3 c = ld3(row);
     const float4* bv = reinterpret_cast<const float4*>(m.body_verts);
@@ -670,7 +696,9 @@ __global__ void diff_force_kernel(mwd_diff d, const double* __restrict__ x, int 
     }
 }
 
-constexpr int DIFF_RB = 128;
+// FP64-heavy row kernels: small blocks spread a few thousand rows over many SMs (GB300's FP64
+// pipe is narrow, so rows per SM, not occupancy, set the time)
+constexpr int DIFF_RB = 32;
 
 __global__ void __launch_bounds__(DIFF_RB) diff_integrate_kernel(mwd_diff d, const double* __restrict__ x, double* xo,
                                                                  double* FT_store, mwd_state mirror, int has_mirror,
@@ -773,12 +801,13 @@ __global__ void diff_mirror_kernel(mwd_diff d, const double* __restrict__ x, mwd
 
 // lam_prev = (d step / d state)^T lam for the integrator part; gFT = gradient on the step's F, T
 __global__ void __launch_bounds__(DIFF_RB) adj_integrate_kernel(mwd_diff d, const double* __restrict__ x,
-                                                                const double* __restrict__ FT, int t,
+                                                                const double* __restrict__ FT, int t_arg,
                                                                 const double* __restrict__ lam, double* lam_prev,
                                                                 const double* __restrict__ com_grad, double* gFT)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= d.n) return;
+    const int t = step_of(d, t_arg);
+    if (r >= d.n || t >= d.n_steps) return;
     double* lp = lam_prev + (size_t)MWD_DIFF_ROW * r;
     double* gft = gFT + 8 * (size_t)r;
     if (d.info[r] & 1) {
@@ -822,9 +851,11 @@ __global__ void __launch_bounds__(DIFF_RB) adj_integrate_kernel(mwd_diff d, cons
     gft[7] = 0.0;
 }
 
-__global__ void adj_force_kernel(mwd_diff d, const double* __restrict__ x, int t, const double* __restrict__ gFT,
+__global__ void adj_force_kernel(mwd_diff d, const double* __restrict__ x, int t_arg, const double* __restrict__ gFT,
                                  double* lam_prev, double* glaw)
 {
+    const int t = step_of(d, t_arg);
+    if (t >= d.n_steps) return;
     const int64_t cnt = log_count(d, t);
     const int64_t off = d.step_off[t];
     double gl[8];
@@ -951,6 +982,7 @@ int mwd_diff_integrate(const mwd_diff* d, const double* x, double* x_out, double
     diff_integrate_kernel<<<blocks, DIFF_RB, 0, reinterpret_cast<cudaStream_t>(stream)>>>(*d, x, x_out, FT_store, m,
                                                                                         mirror ? 1 : 0, t);
     MWD_CUDA(cudaGetLastError());
+    if (mirror && m.xform && m.vert_owner) return launch_world_verts(m, reinterpret_cast<cudaStream_t>(stream));
     return MWD_OK;
 }
 
@@ -966,6 +998,7 @@ int mwd_diff_mirror(const mwd_diff* d, const double* x, mwd_state* mirror, mwd_s
     if (d->n == 0) return MWD_OK;
     diff_mirror_kernel<<<(d->n + 127) / 128, 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(*d, x, *mirror);
     MWD_CUDA(cudaGetLastError());
+    if (mirror->xform && mirror->vert_owner) return launch_world_verts(*mirror, reinterpret_cast<cudaStream_t>(stream));
     return MWD_OK;
 }
 

@@ -322,39 +322,72 @@ __global__ void __launch_bounds__(32) order_crowded_kernel(BroadArgs a)
     }
 }
 
-// every candidate of the row at sorted position t (row r, cell g), passed to sink(A, B)
+// walls of one scene staged as floats (centre + radius, normal) by the append kernel
+constexpr int WALL_STAGE = 16;
+struct WallStage {
+    const float4* c;  // (nw,) centre, bounding radius
+    const float4* n;  // (nw,) normal
+    int scene;        // the scene they belong to (-1: nothing staged)
+    int nw;
+};
+
+// every candidate of the row at sorted position t (row r, cell g), passed to sink(A, B).
+// ws: optional float copies of the row's scene walls for the wall-distance test.
 template <class Sink>
-__device__ __forceinline__ void walk_pairs(const BroadArgs& a, int t, int r, int g, const mwd_scene& sc, Sink&& sink)
+__device__ __forceinline__ void walk_pairs(const BroadArgs& a, int t, int r, int g, const mwd_scene& sc, int scene,
+                                           const WallStage* ws, Sink&& sink)
 {
     const bool cull = a.cull && a.sorted_pos;
-    const float4 me = cull ? a.sorted_pos[t] : make_float4(0.f, 0.f, 0.f, 0.f);
-    // B at sorted position j (-1: a wall row given by B alone)
-    auto put = [&](int A, int B, int j) {
-        // optional exact-outcome filter: pairs the reference's GJK rejects at its first test
-        if (cull) {
-            float4 pb;
-            if (j >= 0) pb = a.sorted_pos[j];
-            else {
-                const double4 w = reinterpret_cast<const double4*>(a.pos)[B];
-                pb = make_float4((float)w.x, (float)w.y, (float)w.z, (float)w.w);
-            }
-            if (spheres_apart_f(me, pb)) return;
-        }
-        sink(A, B);
-    };
-    // wall candidates (MWDiem.py:808-811): pair [particle, wall]
+    const float4 me = a.sorted_pos ? a.sorted_pos[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+    // wall candidates (MWDiem.py:808-811): pair [particle, wall] when |n . (p - c)| < wall_range (FP64)
     if (a.walls) {
-        const dpos p = reinterpret_cast<const dpos*>(a.pos)[r];
-        for (int k = sc.row_begin; k < sc.wall_end; ++k) {
-            const dpos wc = reinterpret_cast<const dpos*>(a.pos)[k];
-            const dpos wn = reinterpret_cast<const dpos*>(a.wall_normal)[k];
-            double s = wn.x * (p.x - wc.x) + wn.y * (p.y - wc.y) + wn.z * (p.z - wc.z);
-            if (fabs(s) < sc.wall_range) put(r, k, -1);
+        if (ws && ws->scene == scene && a.sorted_pos) {
+            // FP32 test with a margin above its rounding error (inputs rounded to float, three products
+            // and two sums: < 6 u |n|_1 sum_i (|p_i| + |c_i|) with u = 2^-24); inside the margin band,
+            // the FP64 test decides
+            const float range = (float)sc.wall_range;
+            for (int k = 0; k < ws->nw; ++k) {
+                const float4 c = ws->c[k], nr = ws->n[k];
+                const float sf = nr.x * (me.x - c.x) + nr.y * (me.y - c.y) + nr.z * (me.z - c.z);
+                const float mg = 1e-6f * ((fabsf(me.x) + fabsf(me.y) + fabsf(me.z) + fabsf(c.x) + fabsf(c.y) + fabsf(c.z)) *
+                                              (fabsf(nr.x) + fabsf(nr.y) + fabsf(nr.z)) +
+                                          range);
+                bool in;
+                if (fabsf(sf) < range - mg) in = true;
+                else if (fabsf(sf) > range + mg) in = false;
+                else {
+                    const int w = sc.row_begin + k;
+                    const dpos p = reinterpret_cast<const dpos*>(a.pos)[r];
+                    const dpos wc = reinterpret_cast<const dpos*>(a.pos)[w];
+                    const dpos wn = reinterpret_cast<const dpos*>(a.wall_normal)[w];
+                    const double s = wn.x * (p.x - wc.x) + wn.y * (p.y - wc.y) + wn.z * (p.z - wc.z);
+                    in = fabs(s) < sc.wall_range;
+                }
+                // optional exact-outcome filter: pairs the reference's GJK rejects at its first test
+                if (in && !(cull && spheres_apart_f(me, c))) sink(r, sc.row_begin + k);
+            }
+        } else {
+            const dpos p = reinterpret_cast<const dpos*>(a.pos)[r];
+            for (int k = sc.row_begin; k < sc.wall_end; ++k) {
+                const dpos wc = reinterpret_cast<const dpos*>(a.pos)[k];
+                const dpos wn = reinterpret_cast<const dpos*>(a.wall_normal)[k];
+                double s = wn.x * (p.x - wc.x) + wn.y * (p.y - wc.y) + wn.z * (p.z - wc.z);
+                if (!(fabs(s) < sc.wall_range)) continue;
+                if (cull) {
+                    const float4 pb = make_float4((float)wc.x, (float)wc.y, (float)wc.z, (float)wc.w);
+                    if (spheres_apart_f(me, pb)) continue;
+                }
+                sink(r, k);
+            }
         }
     }
+    auto put = [&](int B, int j) {
+        if (cull && spheres_apart_f(me, a.sorted_pos[j])) return;
+        sink(r, B);
+    };
     // later members of the same cell, in set order
     const int ce = a.cell_start[g + 1];
-    for (int j = t + 1; j < ce; ++j) put(r, a.sorted[j], j);
+    for (int j = t + 1; j < ce; ++j) put(a.sorted[j], j);
     // forward neighbours
     const int64_t local = (int64_t)g - sc.cell_base;
     const int64_t nx = sc.nx, nxy = sc.nx * sc.ny;
@@ -372,7 +405,7 @@ __device__ __forceinline__ void walk_pairs(const BroadArgs& a, int t, int r, int
     }
 #pragma unroll
     for (int o = 0; o < 7; ++o)
-        for (int j = rs[o]; j < re[o]; ++j) put(r, a.sorted[j], j);
+        for (int j = rs[o]; j < re[o]; ++j) put(a.sorted[j], j);
 }
 
 template <bool EMIT>
@@ -387,36 +420,74 @@ __global__ void pairs_kernel(BroadArgs a)
     }
     const int r = a.sorted[t];
     const int g = a.sorted_cell ? a.sorted_cell[t] : a.cell_of[r];
-    const mwd_scene& sc = a.scenes[scene_of(a, r)];
+    const int scene = scene_of(a, r);
+    const mwd_scene& sc = a.scenes[scene];
     if (EMIT) {
         int64_t out = a.pair_count[t];
         const int64_t cap = a.pair_cap;
         int2* pairs = reinterpret_cast<int2*>(a.pairs);
-        walk_pairs(a, t, r, g, sc, [&](int A, int B) {
+        walk_pairs(a, t, r, g, sc, scene, nullptr, [&](int A, int B) {
             if (out < cap) pairs[out] = make_int2(A, B);
             ++out;
         });
     } else {
         int c = 0;
-        walk_pairs(a, t, r, g, sc, [&](int, int) { ++c; });
+        walk_pairs(a, t, r, g, sc, scene, nullptr, [&](int, int) { ++c; });
         a.pair_count[t] = c;
     }
 }
 
-// count, reserve (one atomic per warp on n_pairs, zeroed by assign_kernel), write
-__global__ void __launch_bounds__(256) pairs_append_kernel(BroadArgs a)
+constexpr int APPEND_THREADS = 128;
+constexpr int APPEND_KEEP = 8;  // pairs a thread keeps from its walk; rows with more walk again
+
+// one walk (the first APPEND_KEEP pairs kept in shared memory), reserve (one atomic per warp on
+// n_pairs, zeroed by assign_kernel), write
+__global__ void __launch_bounds__(APPEND_THREADS) pairs_append_kernel(BroadArgs a)
 {
+    __shared__ int2 keep[APPEND_KEEP][APPEND_THREADS];
+    __shared__ float4 s_wc[WALL_STAGE], s_wn[WALL_STAGE];
+    __shared__ int s_scene, s_nw;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t == 0) *a.n_crowded = 0;  // consumed by the crowded-cell pass, which ran before
     const int n_sorted = a.cell_start[a.total_cells];
     const bool live = t < n_sorted;
-    int r = 0, g = 0, c = 0;
+    // the walls of the scene of the block's first row, as floats
+    if (threadIdx.x == 0) {
+        s_scene = -1;
+        s_nw = 0;
+        const int t0 = blockIdx.x * blockDim.x;
+        if (a.walls && a.sorted_pos && t0 < n_sorted) {
+            const int sc0 = scene_of(a, a.sorted[t0]);
+            const mwd_scene& sc = a.scenes[sc0];
+            const int nw = sc.wall_end - sc.row_begin;
+            if (nw <= WALL_STAGE) {
+                s_scene = sc0;
+                s_nw = nw;
+            }
+        }
+    }
+    __syncthreads();
+    if (s_scene >= 0 && threadIdx.x < s_nw) {
+        const mwd_scene& sc = a.scenes[s_scene];
+        const int w = sc.row_begin + threadIdx.x;
+        const dpos c = reinterpret_cast<const dpos*>(a.pos)[w];
+        const dpos n = reinterpret_cast<const dpos*>(a.wall_normal)[w];
+        s_wc[threadIdx.x] = make_float4((float)c.x, (float)c.y, (float)c.z, (float)c.w);
+        s_wn[threadIdx.x] = make_float4((float)n.x, (float)n.y, (float)n.z, 0.f);
+    }
+    __syncthreads();
+    const WallStage ws = {s_wc, s_wn, s_scene, s_nw};
+    int r = 0, g = 0, c = 0, scene = 0;
     const mwd_scene* sc = nullptr;
     if (live) {
         r = a.sorted[t];
         g = a.sorted_cell ? a.sorted_cell[t] : a.cell_of[r];
-        sc = &a.scenes[scene_of(a, r)];
-        walk_pairs(a, t, r, g, *sc, [&](int, int) { ++c; });
+        scene = scene_of(a, r);
+        sc = &a.scenes[scene];
+        walk_pairs(a, t, r, g, *sc, scene, &ws, [&](int A, int B) {
+            if (c < APPEND_KEEP) keep[c][threadIdx.x] = make_int2(A, B);
+            ++c;
+        });
     }
     const int lane = threadIdx.x & 31;
     int inc = c;
@@ -430,14 +501,20 @@ __global__ void __launch_bounds__(256) pairs_append_kernel(BroadArgs a)
     if (lane == 31 && total > 0) base = atomicAdd(reinterpret_cast<unsigned long long*>(a.n_pairs), (unsigned long long)total);
     base = __shfl_sync(0xffffffffu, base, 31);
     if (!live || c == 0) return;
-    int64_t out = (int64_t)base + inc - c;
+    const int64_t out = (int64_t)base + inc - c;
     const int64_t cap = a.pair_cap;
     if (out + c > cap) set_status(a.status, MWD_ST_PAIR_OVERFLOW);
     int2* pairs = reinterpret_cast<int2*>(a.pairs);
-    walk_pairs(a, t, r, g, *sc, [&](int A, int B) {
-        if (out < cap) pairs[out] = make_int2(A, B);
-        ++out;
-    });
+    const int kept = c < APPEND_KEEP ? c : APPEND_KEEP;
+    for (int i = 0; i < kept; ++i)
+        if (out + i < cap) pairs[out + i] = keep[i][threadIdx.x];
+    if (c > APPEND_KEEP) {
+        int i = 0;
+        walk_pairs(a, t, r, g, *sc, scene, &ws, [&](int A, int B) {
+            if (i >= APPEND_KEEP && out + i < cap) pairs[out + i] = make_int2(A, B);
+            ++i;
+        });
+    }
 }
 
 // wall-major candidates for the reference-layout entry point (MWDiem.py:808-811)
@@ -518,7 +595,7 @@ int launch_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* tmp, int64_
 
 int launch_broad(const BroadArgs& a, cudaStream_t s)
 {
-    const int T = 256;
+    const int T = 128;  // row kernels: 20k rows already span every SM
     const int64_t rows = a.row_hi - a.row_lo;
     if (rows <= 0 || a.total_cells <= 0) {
         MWD_CUDA(cudaMemsetAsync(a.n_pairs, 0, sizeof(int64_t), s));
@@ -532,7 +609,7 @@ int launch_broad(const BroadArgs& a, cudaStream_t s)
     order_crowded_kernel<<<(unsigned)(a.crowded_cap < 1024 ? (a.crowded_cap > 0 ? a.crowded_cap : 1) : 1024), 32, 0, s>>>(a);
     // rows that have a cell are at most `rows`; threads past cell_start[total] exit
     if (a.append) {
-        pairs_append_kernel<<<blocks(rows, T), T, 0, s>>>(a);
+        pairs_append_kernel<<<blocks(rows, APPEND_THREADS), APPEND_THREADS, 0, s>>>(a);
         MWD_CUDA(cudaGetLastError());
         return MWD_OK;
     }

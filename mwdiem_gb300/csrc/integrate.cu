@@ -406,6 +406,14 @@ int launch_verlet_ref(const VerletRefArgs& a, cudaStream_t s)
     return MWD_OK;
 }
 
+int launch_world_verts(const mwd_state& st, cudaStream_t s)
+{
+    if (st.n_verts <= 0) return MWD_OK;
+    world_verts_kernel<<<(st.n_verts + 255) / 256, 256, 0, s>>>(st);
+    MWD_CUDA(cudaGetLastError());
+    return MWD_OK;
+}
+
 int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, cudaStream_t s)
 {
     if (st.n <= 0) return MWD_OK;

@@ -210,42 +210,68 @@ class DiffEngine:
                              lam2=torch.zeros((self.n, DIFF_ROW), **f64),
                              gFT=torch.zeros((self.n, 8), **f64),
                              glaw=torch.zeros(8, **f64),
-                             com_grad=torch.zeros((self.n_steps_max, 4), **f64))
+                             com_grad=torch.zeros((self.n_steps_max, 4), **f64),
+                             t_base=torch.zeros(1, dtype=torch.int32, device=self.device),
+                             graphs={})
         return self._bwd
+
+    def _segment_launches(self, m, with_com):
+        """Backward over steps t_base .. t_base + m - 1: recompute the m states and forces from
+        seg[0] and the topology log, then the transposed steps from the last to the first.  The
+        gradient enters and leaves in lam."""
+        b = self._bwd
+        stream = _dev.stream_handle()
+        seg, FT = b["seg"], b["FT"]
+        d = C.byref(self.d)
+        L = lib()
+        cg = b["com_grad"].data_ptr() if with_com else None
+        for j in range(m):
+            check(L.mwd_diff_force(d, seg[j].data_ptr(), j, stream))
+            check(L.mwd_diff_integrate(d, seg[j].data_ptr(), seg[j + 1].data_ptr(), FT[j].data_ptr(), None, j,
+                                       stream))
+        lam, lam2 = b["lam"], b["lam2"]
+        for j in range(m - 1, -1, -1):
+            check(L.mwd_diff_adjoint(d, seg[j].data_ptr(), FT[j].data_ptr(), j, lam.data_ptr(), lam2.data_ptr(), cg,
+                                     b["gFT"].data_ptr(), b["glaw"].data_ptr(), stream))
+            lam, lam2 = lam2, lam
+        if lam is not b["lam"]:
+            b["lam"].copy_(lam)
 
     def backward(self, g_com=None, g_final=None):
         """Gradients of <g_com, com> + <g_final, final state> with respect to x0 and the law."""
         b = self._bwd_buffers()
-        stream = _dev.stream_handle()
         n_steps, K = self.steps, self.K
-        lam, lam2 = b["lam"], b["lam2"]
         if g_final is not None:
-            lam.copy_(g_final.detach())
+            b["lam"].copy_(g_final.detach())
         else:
-            lam.zero_()
+            b["lam"].zero_()
         b["glaw"].zero_()
-        cg = None
-        if g_com is not None:
+        with_com = g_com is not None
+        if with_com:
             b["com_grad"].zero_()
             b["com_grad"][:n_steps, :3].copy_(g_com.detach())
-            cg = b["com_grad"].data_ptr()
-        seg, FT = b["seg"], b["FT"]
-        d = C.byref(self.d)
-        L = lib()
-        n_seg = (n_steps + K - 1) // K
-        for s in range(n_seg - 1, -1, -1):
-            t0 = s * K
-            t1 = min(t0 + K, n_steps)
-            seg[0].copy_(self.ckpt[s])
-            for j in range(t1 - t0):
-                check(L.mwd_diff_force(d, seg[j].data_ptr(), t0 + j, stream))
-                check(L.mwd_diff_integrate(d, seg[j].data_ptr(), seg[j + 1].data_ptr(), FT[j].data_ptr(), None,
-                                           t0 + j, stream))
-            for j in range(t1 - t0 - 1, -1, -1):
-                check(L.mwd_diff_adjoint(d, seg[j].data_ptr(), FT[j].data_ptr(), t0 + j, lam.data_ptr(),
-                                         lam2.data_ptr(), cg, b["gFT"].data_ptr(), b["glaw"].data_ptr(), stream))
-                lam, lam2 = lam2, lam
-        return lam.clone(), b["glaw"].view(2, 4).clone()
+        self.d.t_base = b["t_base"].data_ptr()
+        try:
+            n_seg = (n_steps + K - 1) // K
+            for s in range(n_seg - 1, -1, -1):
+                t0 = s * K
+                m = min(K, n_steps - t0)
+                b["t_base"].fill_(t0)
+                b["seg"][0].copy_(self.ckpt[s])
+                if self.use_graph and m == K and n_seg > 2:
+                    g = b["graphs"].get(with_com)
+                    if g is None:
+                        torch.cuda.synchronize()
+                        g = torch.cuda.CUDAGraph()
+                        with torch.cuda.graph(g):   # recorded, not run
+                            self._segment_launches(m, with_com)
+                        b["graphs"][with_com] = g
+                    g.replay()
+                else:
+                    self._segment_launches(m, with_com)
+        finally:
+            self.d.t_base = None
+        return b["lam"].clone(), b["glaw"].view(2, 4).clone()
 
 
 class _Rollout(torch.autograd.Function):

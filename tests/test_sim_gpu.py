@@ -171,3 +171,28 @@ def test_sphere_filter_drops_only_noncontacts():
     torch.cuda.synchronize()
     F1, F2 = full.t["force"].cpu().numpy(), cut.t["force"].cpu().numpy()
     assert np.abs(F1 - F2).max() <= 1e-5 * np.abs(F1).max()
+
+
+def test_wall_test_band_defers_to_fp64():
+    # centres placed within float rounding of the wall range (|n . (p - c)| = wall_range + eps): the
+    # device step's FP32 wall test must hand these to its FP64 test and list exactly the wall pairs
+    # of MWDiem.py:808-811
+    from mwdiem_gb300.sim import Simulator
+    sp = scene.pour_scene(n=300, seed=4, box=16.0, spacing=2.6, pool=16)
+    rng = np.random.default_rng(9)
+    floor_c = np.asarray(sp.walls[0][1], float)
+    rng_w = 6.0 * sp.max_particlesize
+    eps = np.array([0.0, 1e-12, -1e-12, 1e-9, -1e-9, 1e-7, -1e-7, 1e-6, -1e-6, 1e-5, -1e-5, 1e-4, -1e-4, 1e-3, -1e-3])
+    k = len(eps) * 4
+    sp.centres = sp.centres.copy()
+    sp.centres[:k, 2] = floor_c[2] + rng_w + np.tile(eps, 4)
+    sp.centres[:k, 0] = rng.uniform(-6, 6, size=k)
+    sp.centres[:k, 1] = rng.uniform(-6, 6, size=k)
+    sim = Simulator(sp, cull_pairs=False)
+    sim.broadphase()
+    got = {tuple(p) for p in sim.pairs().cpu().numpy().tolist() if p[1] < sp.n_walls}
+    ref = stepper.RefStepper(sp)
+    want = {tuple(p) for p in ref.candidate_pairs().tolist() if p[1] < sp.n_walls}
+    assert got == want
+    near = {sp.n_walls + i for i in range(k)}
+    assert {p for p in want if p[0] in near and p[1] == 0}, "the band rows should include floor pairs"
