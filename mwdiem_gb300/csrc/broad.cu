@@ -60,6 +60,8 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* sh, int* total)
 
 __global__ void scan_reduce_kernel(const int32_t* in, int64_t n, int32_t* block_sums)
 {
+    pdl_wait();
+    pdl_launch_dependents();
     __shared__ int sh[SCAN_THREADS / 32];
     int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
     int s = 0;
@@ -77,6 +79,8 @@ __global__ void scan_reduce_kernel(const int32_t* in, int64_t n, int32_t* block_
 __global__ void scan_final_kernel(const int32_t* in, int64_t n, const int32_t* block_sums, int32_t* out, int nb,
                                   int64_t* total_out, int64_t cap, uint32_t* status, uint32_t overflow_bit)
 {
+    pdl_wait();
+    pdl_launch_dependents();
     __shared__ int sh[SCAN_THREADS / 32];
     int part = 0;
     for (int i = threadIdx.x; i < (int)blockIdx.x; i += SCAN_THREADS) part += block_sums[i];
@@ -206,7 +210,12 @@ __device__ __forceinline__ int64_t row_key(const BroadArgs& a, const mwd_scene& 
 
 __global__ void assign_kernel(BroadArgs a)
 {
-    if (a.append && blockIdx.x == 0 && threadIdx.x == 0) *a.n_pairs = 0;  // appended to by pairs_append_kernel
+    pdl_wait();
+    pdl_launch_dependents();
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (a.append) *a.n_pairs = 0;  // appended to by pairs_append_kernel
+        if (a.epa_count) *a.epa_count = 0;
+    }
     const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= a.row_hi) return;
     if (is_wall(a, r)) {
@@ -227,6 +236,8 @@ __global__ void assign_kernel(BroadArgs a)
 
 __global__ void scatter_kernel(BroadArgs a)
 {
+    pdl_wait();
+    pdl_launch_dependents();
     const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= a.row_hi) return;
     const int g = a.cell_of[r];
@@ -248,6 +259,8 @@ __device__ __forceinline__ void place(const BroadArgs& a, int i, int v, int g)
 
 __global__ void order_kernel(BroadArgs a)
 {
+    pdl_wait();
+    pdl_launch_dependents();
     const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= a.row_hi) return;
     const int g = a.cell_of[r];
@@ -287,6 +300,8 @@ __global__ void order_kernel(BroadArgs a)
 // one warp per crowded cell: members ranked by id in parallel, then lane 0 replays the set inserts
 __global__ void __launch_bounds__(32) order_crowded_kernel(BroadArgs a)
 {
+    pdl_wait();
+    pdl_launch_dependents();
     __shared__ int m[BIG_CELL];
     __shared__ int o[BIG_CELL];
     __shared__ int tab[BIG_TAB], tmp[BIG_TAB];
@@ -411,6 +426,8 @@ __device__ __forceinline__ void walk_pairs(const BroadArgs& a, int t, int r, int
 template <bool EMIT>
 __global__ void pairs_kernel(BroadArgs a)
 {
+    pdl_wait();
+    pdl_launch_dependents();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (!EMIT && t == 0) *a.n_crowded = 0;  // consumed by the crowded-cell pass, which ran before
     const int n_sorted = a.cell_start[a.total_cells];
@@ -444,6 +461,8 @@ constexpr int APPEND_KEEP = 8;  // pairs a thread keeps from its walk; rows with
 // n_pairs, zeroed by assign_kernel), write
 __global__ void __launch_bounds__(APPEND_THREADS) pairs_append_kernel(BroadArgs a)
 {
+    pdl_wait();
+    pdl_launch_dependents();
     __shared__ int2 keep[APPEND_KEEP][APPEND_THREADS];
     __shared__ float4 s_wc[WALL_STAGE], s_wn[WALL_STAGE];
     __shared__ int s_scene, s_nw;
@@ -587,8 +606,9 @@ int launch_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* tmp, int64_
 {
     const int nb = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
     const int nbl = nb > 0 ? nb : 1;
-    scan_reduce_kernel<<<nbl, SCAN_THREADS, 0, s>>>(in, n, tmp);
-    scan_final_kernel<<<nbl, SCAN_THREADS, 0, s>>>(in, n, tmp, out, nbl, total_out, cap, status, overflow_bit);
+    MWD_CUDA(launch_pdl(scan_reduce_kernel, nbl, SCAN_THREADS, 0, s, in, n, tmp));
+    MWD_CUDA(launch_pdl(scan_final_kernel, nbl, SCAN_THREADS, 0, s, in, n, tmp, out, nbl, total_out, cap, status,
+                        overflow_bit));
     MWD_CUDA(cudaGetLastError());
     return MWD_OK;
 }
@@ -601,15 +621,16 @@ int launch_broad(const BroadArgs& a, cudaStream_t s)
         MWD_CUDA(cudaMemsetAsync(a.n_pairs, 0, sizeof(int64_t), s));
         return MWD_OK;
     }
-    assign_kernel<<<blocks(rows, T), T, 0, s>>>(a);
+    MWD_CUDA(launch_pdl(assign_kernel, blocks(rows, T), T, 0, s, a));
     int rc = launch_scan(a.cell_count, a.total_cells, a.cell_start, a.scan_tmp, nullptr, INT64_MAX, nullptr, 0, s);
     if (rc) return rc;
-    scatter_kernel<<<blocks(rows, T), T, 0, s>>>(a);
-    order_kernel<<<blocks(rows, T), T, 0, s>>>(a);
-    order_crowded_kernel<<<(unsigned)(a.crowded_cap < 1024 ? (a.crowded_cap > 0 ? a.crowded_cap : 1) : 1024), 32, 0, s>>>(a);
+    MWD_CUDA(launch_pdl(scatter_kernel, blocks(rows, T), T, 0, s, a));
+    MWD_CUDA(launch_pdl(order_kernel, blocks(rows, T), T, 0, s, a));
+    MWD_CUDA(launch_pdl(order_crowded_kernel,
+                        (unsigned)(a.crowded_cap < 1024 ? (a.crowded_cap > 0 ? a.crowded_cap : 1) : 1024), 32, 0, s, a));
     // rows that have a cell are at most `rows`; threads past cell_start[total] exit
     if (a.append) {
-        pairs_append_kernel<<<blocks(rows, APPEND_THREADS), APPEND_THREADS, 0, s>>>(a);
+        MWD_CUDA(launch_pdl(pairs_append_kernel, blocks(rows, APPEND_THREADS), APPEND_THREADS, 0, s, a));
         MWD_CUDA(cudaGetLastError());
         return MWD_OK;
     }

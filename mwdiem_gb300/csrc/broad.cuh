@@ -31,6 +31,7 @@ struct BroadArgs {
     int64_t crowded_cap;
     int32_t* pairs;              // (pair_cap,2)
     int64_t* n_pairs;
+    int32_t* epa_count;          // optional: zeroed by assign_kernel for the narrow phase that follows
     uint32_t* status;
     int64_t total_cells;
     int64_t pair_cap;

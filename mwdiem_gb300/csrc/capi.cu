@@ -5,6 +5,7 @@
 // synchronises the device except mwd_linked_cell_hash, which must read the key range before it
 // can size its cell table.
 #include <math.h>
+#include <stdlib.h>
 #include <stdarg.h>
 #include <stdio.h>
 
@@ -135,6 +136,16 @@ static void derive_one(double Kn, double en, double et, double mu, double dt, mw
 }
 
 }  // namespace mwd
+
+bool mwd::pdl_enabled()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("MWD_PDL");
+        v = (e && e[0] == '0') ? 0 : 1;
+    }
+    return v == 1;
+}
 
 using namespace mwd;
 
@@ -396,13 +407,23 @@ int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_s
     a.pair_cap = work->pair_cap;
     a.cull = work->cull_pairs ? 1 : 0;
     a.append = 1;
+    a.epa_count = work->epa_rec ? work->epa_count : nullptr;
     a.sorted_pos = reinterpret_cast<float4*>(work->sorted_pos);
     a.sorted_cell = work->sorted_cell;
     return launch_broad(a, reinterpret_cast<cudaStream_t>(stream));
 }
 
+static int narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work* work, int32_t lanes,
+                        mwd_stream_t stream, bool epa_zeroed);
+
 int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work* work, int32_t lanes,
                      mwd_stream_t stream)
+{
+    return narrow_force(st, scenes_dev, work, lanes, stream, false);
+}
+
+static int narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work* work, int32_t lanes,
+                        mwd_stream_t stream, bool epa_zeroed)
 {
     if (!st || !scenes_dev || !work) {
         set_error("mwd_narrow_force: bad arguments");
@@ -432,6 +453,7 @@ int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work*
         a.epa_rec = work->epa_rec;
         a.epa_cap = work->epa_cap;
         a.pre_culled = work->cull_pairs ? 1 : 0;
+        a.epa_zeroed = epa_zeroed ? 1 : 0;
         return launch_narrow_two_pass(a, lp | (elp << 8), reinterpret_cast<cudaStream_t>(stream));
     }
     return launch_narrow(a, 1, lp, -1, reinterpret_cast<cudaStream_t>(stream));
@@ -452,7 +474,8 @@ int mwd_step(mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes
     for (int i = 0; i < n_steps; ++i) {
         int rc = mwd_broadphase(st, scenes_dev, scenes_host, n_scenes, work, stream);
         if (rc) return rc;
-        rc = mwd_narrow_force(st, scenes_dev, work, lanes, stream);
+        // the broad phase zeroed the EPA counter (assign_kernel): no memset node between the kernels
+        rc = narrow_force(st, scenes_dev, work, lanes, stream, true);
         if (rc) return rc;
         rc = mwd_integrate(st, scenes_dev, work->status, stream);
         if (rc) return rc;

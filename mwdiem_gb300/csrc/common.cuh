@@ -93,6 +93,31 @@ namespace mwd {
 void set_error(const char* fmt, ...);
 int cuda_check(cudaError_t e, const char* what);
 int num_sms();
+
+// Programmatic dependent launch.  The kernels of the device step are launched with launch_pdl: the
+// next kernel's blocks may be scheduled while the previous kernel drains, and each of those kernels
+// calls pdl_wait() before it reads anything (the wait returns once every earlier grid of the stream
+// has completed and its writes are visible), then pdl_launch_dependents() so its own successor can
+// be scheduled as soon as all of its blocks run.  MWD_PDL=0 in the environment turns it off.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+bool pdl_enabled();
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
 }  // namespace mwd
 
 #define MWD_CUDA(call)                                                  \

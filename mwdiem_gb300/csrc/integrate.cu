@@ -323,6 +323,8 @@ __device__ __forceinline__ float4 world_vertex(const float* R, const float* c, f
 __global__ void __launch_bounds__(RB) integrate_kernel(mwd_state st, const mwd_scene* __restrict__ scenes,
                                                        uint32_t* status)
 {
+    pdl_wait();
+    pdl_launch_dependents();
     __shared__ float s_R[RB][9];
     __shared__ float s_c[RB][6];  // centre split hi/lo per axis
     __shared__ int s_off[RB + 1];
@@ -368,6 +370,8 @@ __global__ void __launch_bounds__(RB) integrate_kernel(mwd_state st, const mwd_s
 __global__ void __launch_bounds__(RB) integrate_rows_kernel(mwd_state st, const mwd_scene* __restrict__ scenes,
                                                             uint32_t* status)
 {
+    pdl_wait();
+    pdl_launch_dependents();
     const int P = blockIdx.x * RB + threadIdx.x;
     if (P >= st.n) return;
     dpos pos;
@@ -386,6 +390,8 @@ __global__ void __launch_bounds__(RB) integrate_rows_kernel(mwd_state st, const 
 // the vertex pass of the split integrator: one thread per vertex
 __global__ void __launch_bounds__(256) world_verts_kernel(mwd_state st)
 {
+    pdl_wait();
+    pdl_launch_dependents();
     const int j = blockIdx.x * 256 + threadIdx.x;
     if (j >= st.n_verts) return;
     const int o = st.vert_owner[j];
@@ -409,8 +415,7 @@ int launch_verlet_ref(const VerletRefArgs& a, cudaStream_t s)
 int launch_world_verts(const mwd_state& st, cudaStream_t s)
 {
     if (st.n_verts <= 0) return MWD_OK;
-    world_verts_kernel<<<(st.n_verts + 255) / 256, 256, 0, s>>>(st);
-    MWD_CUDA(cudaGetLastError());
+    MWD_CUDA(launch_pdl(world_verts_kernel, (st.n_verts + 255) / 256, 256, 0, s, st));
     return MWD_OK;
 }
 
@@ -418,10 +423,10 @@ int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* sta
 {
     if (st.n <= 0) return MWD_OK;
     if (st.vert_owner && st.xform) {
-        integrate_rows_kernel<<<(st.n + RB - 1) / RB, RB, 0, s>>>(st, scenes, status);
-        if (st.n_verts > 0) world_verts_kernel<<<(st.n_verts + 255) / 256, 256, 0, s>>>(st);
+        MWD_CUDA(launch_pdl(integrate_rows_kernel, (st.n + RB - 1) / RB, RB, 0, s, st, scenes, status));
+        if (st.n_verts > 0) MWD_CUDA(launch_pdl(world_verts_kernel, (st.n_verts + 255) / 256, 256, 0, s, st));
     } else {
-        integrate_kernel<<<(st.n + RB - 1) / RB, RB, 0, s>>>(st, scenes, status);
+        MWD_CUDA(launch_pdl(integrate_kernel, (st.n + RB - 1) / RB, RB, 0, s, st, scenes, status));
     }
     MWD_CUDA(cudaGetLastError());
     return MWD_OK;

@@ -750,6 +750,8 @@ __device__ int gjk_decide(const Group<LPP>& g, const float4* hA, int nA, const f
 template <int LPP>
 __global__ void __launch_bounds__(NARROW_THREADS, 6) gjk_pass_kernel(NarrowArgs a)
 {
+    pdl_wait();
+    pdl_launch_dependents();
     constexpr int GPB = NARROW_THREADS / LPP;
     const int grp = threadIdx.x / LPP;
     Group<LPP> g;
@@ -826,6 +828,8 @@ __global__ void __launch_bounds__(NARROW_THREADS, 6) gjk_pass_kernel(NarrowArgs 
 template <int LPP>
 __global__ void __launch_bounds__(NARROW_THREADS) epa_pass_kernel(NarrowArgs a)
 {
+    pdl_wait();
+    pdl_launch_dependents();
     extern __shared__ float4 smem[];
     constexpr int GPB = NARROW_THREADS / LPP;
     const int grp = threadIdx.x / LPP;
@@ -904,10 +908,9 @@ int launch_two_pass_lpp(const NarrowArgs& a, cudaStream_t s)
         epa_per_sm = v < 1 ? 1 : v;
         epa_shm_cached = shm;
     }
-    MWD_CUDA(cudaMemsetAsync(a.epa_count, 0, sizeof(int32_t), s));
-    gjk_pass_kernel<LPP><<<(unsigned)(num_sms() * gjk_per_sm), NARROW_THREADS, 0, s>>>(a);
-    epa_pass_kernel<ELPP><<<(unsigned)(num_sms() * epa_per_sm), NARROW_THREADS, shm, s>>>(a);
-    MWD_CUDA(cudaGetLastError());
+    if (!a.epa_zeroed) MWD_CUDA(cudaMemsetAsync(a.epa_count, 0, sizeof(int32_t), s));
+    MWD_CUDA(launch_pdl(gjk_pass_kernel<LPP>, (unsigned)(num_sms() * gjk_per_sm), NARROW_THREADS, 0, s, a));
+    MWD_CUDA(launch_pdl(epa_pass_kernel<ELPP>, (unsigned)(num_sms() * epa_per_sm), NARROW_THREADS, shm, s, a));
     return MWD_OK;
 }
 

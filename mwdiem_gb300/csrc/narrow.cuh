@@ -42,7 +42,7 @@ struct NarrowArgs {
     void* epa_rec;          // (epa_cap,) 80-byte records
     int64_t epa_cap;
     int32_t pre_culled;     // the pair list holds only pairs whose bounding spheres overlap
-    int32_t pad2;
+    int32_t epa_zeroed;     // 1: epa_count was zeroed by an earlier kernel of the stream (the broad phase)
 };
 
 int launch_narrow(const NarrowArgs& a, int mode, int lanes, int64_t n_hint, cudaStream_t s);
