@@ -37,7 +37,7 @@ struct EpaMem {
     uint32_t ft[FCAP];     // T0 | T1 << 8 | T2 << 16 | (valid + 2) << 24
     float4 pv[VCAP];       // polytope vertices
     uint16_t pab[VCAP];    // support index on A | on B << 8
-    uint8_t del[FCAP];     // faces deleted in this iteration, in index order
+    uint32_t del[FCAP];    // faces deleted in this iteration, in index order: vertices T0 T1 T2 | face << 24
 };
 
 __device__ __forceinline__ int ft_v(uint32_t t, int k) { return (t >> (8 * k)) & 0xff; }
@@ -60,6 +60,25 @@ struct Group {
     }
     __device__ __forceinline__ unsigned lt_mask() const { return (1u << lane) - 1u; }
 };
+
+// Order-preserving key of a float (-0 and +0 share the key of +0, as they compare equal): the
+// group reductions below run on these keys with redux.sync.
+__device__ __forceinline__ unsigned fkey(float f)
+{
+    f = (f == 0.f) ? 0.f : f;
+    const unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+// Group-wide (largest value, then smallest index) of the lanes' (v, i), v not NaN: the sequential
+// "v > best" scan's first-index result when each lane holds its own first-index best.
+template <int LPP>
+__device__ __forceinline__ int group_argmax(const Group<LPP>& g, float v, int i)
+{
+    const unsigned k = fkey(v);
+    const unsigned km = __reduce_max_sync(g.mask, k);
+    return (int)__reduce_min_sync(g.mask, k == km ? (unsigned)i : 0xffffffffu);
+}
 
 // argmax of d.a over A and of (-d).b over B, first index on ties (.cu:55-101)
 // work counted per pair when the caller asks for it: vertex dot products, EPA faces, support queries
@@ -86,15 +105,8 @@ __device__ __forceinline__ void support(const Group<LPP>& g, const float4* hA, i
         float t = nd.x * v.x + nd.y * v.y + nd.z * v.z;
         if (t > bB) { bB = t; iB = j; }
     }
-#pragma unroll
-    for (int off = LPP / 2; off > 0; off >>= 1) {
-        float ov = __shfl_xor_sync(g.mask, bA, off, LPP);
-        int oi = __shfl_xor_sync(g.mask, iA, off, LPP);
-        if (ov > bA || (ov == bA && oi < iA)) { bA = ov; iA = oi; }
-        float ow = __shfl_xor_sync(g.mask, bB, off, LPP);
-        int oj = __shfl_xor_sync(g.mask, iB, off, LPP);
-        if (ow > bB || (ow == bB && oj < iB)) { bB = ow; iB = oj; }
-    }
+    iA = group_argmax<LPP>(g, bA, iA);
+    iB = group_argmax<LPP>(g, bB, iB);
     ia = iA;
     ib = iB;
     float4 a = hA[iA], b = hB[iB];
@@ -246,11 +258,11 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
             float v = m.fn[f].w;
             if (min_better(v, f, bv, bi)) { bv = v; bi = f; }
         }
-#pragma unroll
-        for (int off = LPP / 2; off > 0; off >>= 1) {
-            float ov = __shfl_xor_sync(g.mask, bv, off, LPP);
-            int oi = __shfl_xor_sync(g.mask, bi, off, LPP);
-            if (min_better(ov, oi, bv, bi)) { bv = ov; bi = oi; }
+        {
+            // group minimum (NaN never wins), then the first face index holding it
+            const unsigned k = (bv != bv) ? 0xffffffffu : fkey(bv);
+            const unsigned km = __reduce_min_sync(g.mask, k);
+            bi = (int)__reduce_min_sync(g.mask, k == km ? (unsigned)bi : 0xffffffffu);
         }
         float d0 = m.fn[0].w;
         indmin = (d0 != d0) ? 0 : bi;
@@ -277,8 +289,9 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
         for (int base = 0; base < nt; base += LPP) {
             int f = base + g.lane;
             bool dead = false;
+            uint32_t t = 0;
             if (f < nt) {
-                uint32_t t = m.ft[f];
+                t = m.ft[f];
                 int vl = ft_valid(t);
                 if ((vl == 1 || vl == -2) && dot(s - xyz(m.pv[ft_v(t, 0)]), xyz(m.fn[f])) >= 0.f) {
                     dead = true;
@@ -286,7 +299,7 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
                 }
             }
             unsigned b = g.ballot(dead);
-            if (dead) m.del[ndel + __popc(b & g.lt_mask())] = (uint8_t)f;
+            if (dead) m.del[ndel + __popc(b & g.lt_mask())] = (t & 0x00ffffffu) | ((uint32_t)f << 24);
             ndel += __popc(b);
         }
         g.sync();
@@ -299,13 +312,13 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
             bool keep = false;
             int e0 = 0, e1 = 0;
             if (c < 3 * ndel) {
-                uint32_t t = m.ft[m.del[c / 3]];
+                uint32_t t = m.del[c / 3];
                 int k = c % 3;
                 e0 = ft_v(t, k);
                 e1 = ft_v(t, k == 2 ? 0 : k + 1);
                 int cnt = 0;
                 for (int j = 0; j < ndel; ++j) {
-                    uint32_t u = m.ft[m.del[j]];
+                    uint32_t u = m.del[j];
                     int x = ft_v(u, 0), y = ft_v(u, 1), z = ft_v(u, 2);
                     cnt += (e0 == y && e1 == x) + (e0 == x && e1 == y) + (e0 == z && e1 == y) +
                            (e0 == y && e1 == z) + (e0 == x && e1 == z) + (e0 == z && e1 == x);
@@ -322,7 +335,7 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
         if (nt + nnew > FCAP) overflow = true;
         g.sync();
         for (int k = g.lane; k < ndel; k += LPP) {
-            int f = m.del[k];
+            int f = (int)(m.del[k] >> 24);
             m.ft[f] = (m.ft[f] & 0x00ffffffu) | ((uint32_t)(0 + 2) << 24);
             m.fn[f].w = 3e20f;
         }
