@@ -356,7 +356,7 @@ def breakdown(sim, V, flush, reps=10):
     dom = max(ms, key=ms.get)
     if dom == "narrow":
         a = flops / (ms["narrow"] * 1e-3) / 1e12
-        roof = {"kernel": "narrow_kernel<8,1>", "bound": "fp32", "achieved": a, "peak": fp32_peak,
+        roof = {"kernel": "gjk_pass_kernel + epa_pass_kernel", "bound": "fp32", "achieved": a, "peak": fp32_peak,
                 "unit": "TFLOP/s", "frac": a / fp32_peak if fp32_peak else None, "traffic": None,
                 "peak_source": "measured in this run (mwd_probe_fp32: FMUL+FADD chains, no FMA)"}
     elif dom == "integrate":
@@ -376,7 +376,47 @@ def breakdown(sim, V, flush, reps=10):
     return out, roof
 
 
-def pairs_rate(n_pairs, lanes, reps=5):
+def pairs_cpu_rate(ps, n_pairs, sample=30_000, max_seconds=20.0):
+    """Pairs/s of the reference's contact kernel on the host (its own source compiled for the host,
+    all cores; else the oracle's restatement, one core) on a random sample of the same pairs.  The
+    reference's EPA writes past its 50-face arrays on some deep overlaps (its host build then
+    crashes), so the sample keeps the pairs the oracle finishes within 50 faces."""
+    import numpy as np
+    import oracle
+    k = min(n_pairs, sample)
+    idx = np.sort(np.random.default_rng(0).choice(n_pairs, size=k, replace=False))
+    inp = ps.gather(idx)
+    inp["A_id"] = (2 * np.arange(k)).astype(np.int32)
+    inp["B_id"] = (2 * np.arange(k) + 1).astype(np.int32)
+    params = dict(ps.params, num_particles_wall=0)
+    # the pairs whose EPA stays within the reference's 50 faces (oracle with that capacity, clean status)
+    ok = np.nonzero(oracle.contact(inp, params, 2 * k, "f32", face_cap=50)["status"] == 0)[0]
+    inp = {kk: np.ascontiguousarray(v[ok]) for kk, v in inp.items()}
+    inp["A_id"] = (2 * np.arange(len(ok))).astype(np.int32)
+    inp["B_id"] = (2 * np.arange(len(ok)) + 1).astype(np.int32)
+    dropped = k - len(ok)
+    k = len(ok)
+    kind, cores = "reference", os.cpu_count() or 1
+    try:
+        ref = oracle.RefContact(params, "f32")
+        run = lambda d: ref.run(d, 2 * k, nthreads=cores)  # noqa: E731
+        run({kk: v[:64] for kk, v in inp.items()})
+    except Exception:
+        kind, cores = "port", 1
+        run = lambda d: oracle.contact(d, params, 2 * k, "f32")  # noqa: E731
+    done, t0 = 0, time.perf_counter()
+    for a in range(0, k, 10_000):
+        run({kk: v[a:a + 10_000] for kk, v in inp.items()})
+        done += min(10_000, k - a)
+        if time.perf_counter() - t0 > max_seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": "pairs/s", "cores": cores, "kind": kind,
+            "sample": f"{done} of the {n_pairs} pairs (random, same seed; {dropped} pairs whose EPA overruns the "
+                      f"reference's 50 faces or stops at its iteration cap left out), in chunks of 10,000"}
+
+
+def pairs_rate(n_pairs, lanes, reps=5, with_cpu=True):
     """GJK/EPA pairs/s of the device-step narrow phase on independent random pairs (hulls of 8-64
     vertices, radius U[0.8,1.2], centre distance U[0.5,2.2] (rA+rB)/2; inputs ~10 GB, far above L2)."""
     import ctypes as C
@@ -412,7 +452,8 @@ def pairs_rate(n_pairs, lanes, reps=5):
     tf = C.c_double(0)
     _lib.check(_lib.lib().mwd_probe_fp32(20000, scratch.data_ptr(), C.byref(tf), None))
     ach = flops / (ms * 1e-3) / 1e12
-    return {"pairs": n_pairs, "ms_per_launch": ms, "pairs_per_s": n_pairs / (ms * 1e-3),
+    cpu = pairs_cpu_rate(ps, n_pairs) if with_cpu else None
+    return {"pairs": n_pairs, "ms_per_launch": ms, "pairs_per_s": n_pairs / (ms * 1e-3), "cpu_baseline": cpu,
             "contact_fraction": float((coll == 1).mean()), "support_queries": queries, "vertex_dots": dots,
             "epa_faces": faces, "lanes_per_pair": best, "lanes_sweep_ms": sweep, "two_pass": True,
             "roofline": {"kernel": "gjk_pass + epa_pass", "bound": "fp32", "achieved": ach, "peak": tf.value,

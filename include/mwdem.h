@@ -260,7 +260,15 @@ typedef struct {
     int64_t pair_cap;
     int32_t* face_ids;     /* optional (pair_cap, 6): support-vertex indices (into each row's vertex table)
                               of the final EPA face, A's three then B's, written where collision is 1 */
+    int32_t deterministic; /* 1: the pair list is built in cell order and each particle's force and torque
+                              are summed in pair-list order (as a serial loop over the pairs adds them)
+                              instead of with float atomics; needs epa_rec and det_scratch */
+    int32_t pad2;
+    void* det_scratch;     /* (mwd_det_scratch_bytes(n, epa_cap),) zeroed before the first step */
 } mwd_work;
+
+/* Scratch bytes of the deterministic accumulation for n rows and epa_cap contacts. */
+int64_t mwd_det_scratch_bytes(int32_t n, int64_t epa_cap);
 
 /* Scratch ints the device-wide scans need for arrays of n elements. */
 int64_t mwd_scan_tmp_ints(int64_t n);

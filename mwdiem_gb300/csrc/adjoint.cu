@@ -939,7 +939,7 @@ int mwd_diff_collect(const mwd_diff* d, const mwd_work* work, mwd_stream_t strea
     }
     if (work->pair_cap == 0) return MWD_OK;
     int64_t b = (work->pair_cap + 255) / 256;
-    const int64_t cap = (int64_t)num_sms() * 8;
+    const int64_t cap = (int64_t)num_sms() * 2;
     if (b > cap) b = cap;
     diff_collect_kernel<<<(int)b, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
         *d, reinterpret_cast<const int2*>(work->pairs), work->n_pairs, work->collision, work->face_ids);
@@ -954,8 +954,8 @@ int mwd_diff_force(const mwd_diff* d, const double* x, int32_t t, mwd_stream_t s
         set_error("mwd_diff_force: bad arguments");
         return MWD_ERR_INVALID;
     }
-    // the contact count lives on the device: a grid over all SMs strides through the step's records
-    diff_force_kernel<<<num_sms() * 4, 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(*d, x, t);
+    // the contact count lives on the device: one block per SM strides through the step's records
+    diff_force_kernel<<<num_sms(), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(*d, x, t);
     MWD_CUDA(cudaGetLastError());
     return MWD_OK;
 }
@@ -1014,7 +1014,7 @@ int mwd_diff_adjoint(const mwd_diff* d, const double* x, const double* FT, int32
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     adj_integrate_kernel<<<(d->n + DIFF_RB - 1) / DIFF_RB, DIFF_RB, 0, s>>>(*d, x, FT, t, lam, lam_prev, com_grad, gFT);
     MWD_CUDA(cudaGetLastError());
-    adj_force_kernel<<<num_sms() * 2, 128, 0, s>>>(*d, x, t, gFT, lam_prev, glaw);
+    adj_force_kernel<<<num_sms(), 128, 0, s>>>(*d, x, t, gFT, lam_prev, glaw);
     MWD_CUDA(cudaGetLastError());
     return MWD_OK;
 }

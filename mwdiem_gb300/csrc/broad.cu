@@ -76,6 +76,56 @@ __global__ void scan_reduce_kernel(const int32_t* in, int64_t n, int32_t* block_
 
 // out[i] = sum(in[0..i)), out[n] = total; in and out may alias.  Each block adds up the tile totals
 // of the blocks before it (at most a few thousand values), so no separate pass scans the totals.
+// exclusive scan of up to SCAN_SMALL_MAX elements by one block (one launch instead of two)
+constexpr int SCAN_SMALL_THREADS = 1024;
+constexpr int64_t SCAN_SMALL_MAX = 64 * SCAN_SMALL_THREADS;
+__global__ void __launch_bounds__(SCAN_SMALL_THREADS) scan_small_kernel(const int32_t* in, int64_t n, int32_t* out,
+                                                                        int64_t* total_out, int64_t cap,
+                                                                        uint32_t* status, uint32_t overflow_bit)
+{
+    pdl_wait();
+    pdl_launch_dependents();
+    __shared__ int sh[SCAN_SMALL_THREADS / 32];
+    const int per = (int)((n + SCAN_SMALL_THREADS - 1) / SCAN_SMALL_THREADS);
+    const int64_t base = (int64_t)threadIdx.x * per;
+    int sum = 0;
+    for (int k = 0; k < per; ++k)
+        if (base + k < n) sum += in[base + k];
+    // block scan of the per-thread sums (SCAN_SMALL_THREADS / 32 warps)
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int w = sh[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        sh[lane] = w;
+    }
+    __syncthreads();
+    int ex = (wid ? sh[wid - 1] : 0) + x - sum;
+    for (int k = 0; k < per; ++k) {
+        if (base + k >= n) break;
+        const int v = in[base + k];
+        out[base + k] = ex;
+        ex += v;
+    }
+    if (threadIdx.x == 0) {
+        const int64_t t = sh[SCAN_SMALL_THREADS / 32 - 1];
+        out[n] = (int32_t)t;
+        if (total_out) *total_out = t < cap ? t : cap;
+        if (t > cap) set_status(status, overflow_bit);
+    }
+}
+
 __global__ void scan_final_kernel(const int32_t* in, int64_t n, const int32_t* block_sums, int32_t* out, int nb,
                                   int64_t* total_out, int64_t cap, uint32_t* status, uint32_t overflow_bit)
 {
@@ -604,6 +654,11 @@ int64_t scan_tmp_ints(int64_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 2; }
 int launch_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* tmp, int64_t* total_out, int64_t cap,
                 uint32_t* status, uint32_t overflow_bit, cudaStream_t s)
 {
+    if (n <= SCAN_SMALL_MAX) {
+        MWD_CUDA(launch_pdl(scan_small_kernel, 1, SCAN_SMALL_THREADS, 0, s, in, n, out, total_out, cap, status,
+                            overflow_bit));
+        return MWD_OK;
+    }
     const int nb = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
     const int nbl = nb > 0 ? nb : 1;
     MWD_CUDA(launch_pdl(scan_reduce_kernel, nbl, SCAN_THREADS, 0, s, in, n, tmp));

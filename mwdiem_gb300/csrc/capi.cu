@@ -15,6 +15,7 @@
 #include "broad.cuh"
 #include "common.cuh"
 #include "integrate.cuh"
+#include "reduce.cuh"
 #include "narrow.cuh"
 
 namespace mwd {
@@ -90,17 +91,6 @@ int scratch(size_t bytes, void** out)
 }
 
 // carve aligned sub-buffers out of one allocation
-struct Carver {
-    size_t off = 0;
-    template <class T>
-    size_t take(size_t count)
-    {
-        size_t o = (off + 255) & ~size_t(255);
-        off = o + count * sizeof(T);
-        return o;
-    }
-};
-
 int check_lanes(int lanes, int* out)
 {
     if (lanes == 0) lanes = 8;
@@ -155,6 +145,10 @@ const char* mwd_last_error(void) { return g_err; }
 int mwd_version(void) { return 1; }
 int32_t mwd_num_sms(void) { return num_sms(); }
 int64_t mwd_scan_tmp_ints(int64_t n) { return scan_tmp_ints(n); }
+int64_t mwd_det_scratch_bytes(int32_t n, int64_t epa_cap)
+{
+    return n < 0 || epa_cap < 0 ? -1 : (int64_t)det_scratch_bytes(n, epa_cap);
+}
 
 int mwd_derive_material(const mwd_contact_params* prm, mwd_material m[2])
 {
@@ -406,7 +400,7 @@ int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_s
     a.total_cells = work->total_cells;
     a.pair_cap = work->pair_cap;
     a.cull = work->cull_pairs ? 1 : 0;
-    a.append = 1;
+    a.append = work->deterministic ? 0 : 1;  // deterministic: the list in cell order
     a.epa_count = work->epa_rec ? work->epa_count : nullptr;
     a.sorted_pos = reinterpret_cast<float4*>(work->sorted_pos);
     a.sorted_cell = work->sorted_cell;
@@ -454,7 +448,28 @@ static int narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_wo
         a.epa_cap = work->epa_cap;
         a.pre_culled = work->cull_pairs ? 1 : 0;
         a.epa_zeroed = epa_zeroed ? 1 : 0;
+        if (work->deterministic) {
+            if (!work->det_scratch) {
+                set_error("deterministic accumulation needs work->det_scratch");
+                return MWD_ERR_INVALID;
+            }
+            DetArgs d = det_carve(work->det_scratch, st->n, work->epa_cap);
+            d.pairs = work->pairs;
+            d.recs = reinterpret_cast<const SimplexRec*>(work->epa_rec);
+            d.epa_count = work->epa_count;
+            d.info = st->info;
+            d.force = st->force;
+            d.torque = st->torque;
+            a.det_out = d.out;
+            rc = launch_narrow_two_pass(a, lp | (elp << 8), reinterpret_cast<cudaStream_t>(stream));
+            if (rc) return rc;
+            return launch_det_reduce(d, reinterpret_cast<cudaStream_t>(stream));
+        }
         return launch_narrow_two_pass(a, lp | (elp << 8), reinterpret_cast<cudaStream_t>(stream));
+    }
+    if (work->deterministic) {
+        set_error("deterministic accumulation needs the two-pass narrow phase (work->epa_rec)");
+        return MWD_ERR_UNSUPPORTED;
     }
     return launch_narrow(a, 1, lp, -1, reinterpret_cast<cudaStream_t>(stream));
 }

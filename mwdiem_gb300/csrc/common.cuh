@@ -103,6 +103,18 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
 __device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 bool pdl_enabled();
 
+// offsets of 256-byte aligned sub-arrays in one scratch allocation
+struct Carver {
+    size_t off = 0;
+    template <class T>
+    size_t take(size_t count)
+    {
+        size_t o = (off + 255) & ~size_t(255);
+        off = o + count * sizeof(T);
+        return o;
+    }
+};
+
 template <typename... KArgs, typename... Args>
 cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args)
 {

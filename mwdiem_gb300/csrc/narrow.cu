@@ -707,13 +707,6 @@ __global__ void __launch_bounds__(NARROW_THREADS) narrow_kernel(NarrowArgs a)
 // stopped -- CorrectFlat, EPA, force -- for the listed pairs only, with the shared-memory polytope.
 // The operation sequence per pair is the single-pass kernel's.
 
-struct SimplexRec {
-    float4 S[4];     // simplex points (w unused)
-    int64_t P;       // pair index
-    uint32_t ia;     // support indices on A, 8 bits each
-    uint32_t ib;     // support indices on B
-};
-
 // GJK up to the decision (.cu:996-1288): 0 separated, 1 in contact (simplex in rec), -1 undecided
 // after 50 tetrahedron iterations.
 template <int LPP>
@@ -878,7 +871,14 @@ __global__ void __launch_bounds__(NARROW_THREADS) epa_pass_kernel(NarrowArgs a)
                       p.IsB, fo);
         if (g.lane == 0) {
             set_status(a.status, er.status);
-            accumulate<1>(a, p, fo);
+            if (a.det_out) {
+                float4* o = a.det_out + 3 * i;
+                o[0] = f4(fo.F, 0.f);
+                o[1] = f4(fo.TA, 0.f);
+                o[2] = f4(fo.TB, 0.f);
+            } else {
+                accumulate<1>(a, p, fo);
+            }
             if (a.face_ids) {
                 int* fid = a.face_ids + 6 * P;
                 for (int k = 0; k < 3; ++k) {

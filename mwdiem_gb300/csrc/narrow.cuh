@@ -7,6 +7,14 @@ namespace mwd {
 
 constexpr int NARROW_THREADS = 128;
 
+// a pair the GJK pass found in contact, with the simplex it stopped on (the EPA pass's input)
+struct SimplexRec {
+    float4 S[4];     // simplex points (w unused)
+    int64_t P;       // pair index
+    uint32_t ia;     // support indices on A, 8 bits each
+    uint32_t ib;     // support indices on B
+};
+
 struct NarrowArgs {
     // mode 0: per-pair arrays in the reference's layout
     const float *A_com, *B_com, *A_verts, *B_verts, *A_vel, *B_vel, *A_w, *B_w, *qA, *qB, *IsA, *IsB;
@@ -43,6 +51,7 @@ struct NarrowArgs {
     int64_t epa_cap;
     int32_t pre_culled;     // the pair list holds only pairs whose bounding spheres overlap
     int32_t epa_zeroed;     // 1: epa_count was zeroed by an earlier kernel of the stream (the broad phase)
+    float4* det_out;        // deterministic mode: (epa_cap, 3) F, TA, TB per EPA record instead of atomics
 };
 
 int launch_narrow(const NarrowArgs& a, int mode, int lanes, int64_t n_hint, cudaStream_t s);

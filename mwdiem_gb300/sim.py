@@ -37,7 +37,7 @@ class Layout:
 
 class Simulator:
     def __init__(self, scenes, lanes=8, pair_cap=None, device="cuda", collect_collisions=False, two_pass=True,
-                 cull_pairs=True):
+                 cull_pairs=True, deterministic=False):
         _dev.require_cuda()
         if isinstance(scenes, SceneSpec):
             scenes = [scenes]
@@ -48,6 +48,9 @@ class Simulator:
         self._build_scenes()
         self.two_pass = bool(two_pass)
         self.cull_pairs = bool(cull_pairs)
+        self.deterministic = bool(deterministic)
+        if self.deterministic and not self.two_pass:
+            raise ValueError("deterministic accumulation needs the two-pass narrow phase")
         self._build_work(pair_cap, collect_collisions)
         self.graph = None
         self.graph_steps = 0
@@ -280,6 +283,11 @@ class Simulator:
         w["sorted_cell"] = torch.zeros(n, **i32)
         wk.sorted_pos = w["sorted_pos"].data_ptr()
         wk.sorted_cell = w["sorted_cell"].data_ptr()
+        if self.deterministic:
+            nb = int(lib().mwd_det_scratch_bytes(n, cap))
+            w["det_scratch"] = torch.zeros(nb, dtype=torch.uint8, device=self.device)
+            wk.deterministic = 1
+            wk.det_scratch = w["det_scratch"].data_ptr()
         wk.total_cells = self.total_cells
         wk.pair_cap = cap
         self.work = wk

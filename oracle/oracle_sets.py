@@ -44,10 +44,20 @@ def pour_sets(n=20000, box=40.0, spacing=2.6, r_max=1.2, zeta=0.3, kn=1e5, mu=0.
     return c, v
 
 
+def pairs_set(kn=1e5, zeta=0.3, mu=0.5, dt=5e-5, V=64):
+    """Contact parameters of the independent-pair narrow-phase workload (hulls of up to 64 vertices,
+    no walls), as mwdiem_gb300.pairbench.PairScene sets them."""
+    from mwdiem_gb300 import scene
+    en = scene.restitution_from_damping(zeta)
+    return dict(Kn=kn, en=en, et=en, mu=mu, Kn_wall=kn, en_wall=en, et_wall=en, mu_wall=mu, num_vertices_max=V,
+                num_particles_wall=0, timestep=dt)
+
+
 def render_all():
     c, v = pour_sets()
     register_contact(c)
     register_verlet(v)
+    register_contact(pairs_set())
     out = []
     for p in CONTACT_SETS:
         out.append(build_ref.ensure_built("contact", p, "f32"))
