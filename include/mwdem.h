@@ -43,7 +43,8 @@ enum {
     MWD_ST_BAD_SHAPE = 64u,     /* a hull with more vertices than the staging capacity */
     MWD_ST_DEGENERATE_FACE = 128u, /* differentiable step: a logged contact face of zero area (skipped) */
     MWD_ST_LOG_OVERFLOW = 256u,    /* differentiable step: more contacts than the topology log holds */
-    MWD_ST_FLY_RESET = 512u        /* differentiable step: a particle left the box and was stopped */
+    MWD_ST_FLY_RESET = 512u,       /* differentiable step: a particle left the box and was stopped */
+    MWD_ST_HIST_OVERFLOW = 1024u   /* persistent history: more contacts than the history table holds */
 };
 
 #define MWD_EPA_FACE_CAP 128   /* append-only EPA face list per pair */
@@ -265,6 +266,16 @@ typedef struct {
                               instead of with float atomics; needs epa_rec and det_scratch */
     int32_t pad2;
     void* det_scratch;     /* (mwd_det_scratch_bytes(n, epa_cap),) zeroed before the first step */
+    /* Persistent tangential history (optional; needs epa_rec).  The reference drops every stored
+     * history each step (MWDiem.py:953-966), so its contacts always start from zero.  With these set,
+     * the history of each pair in contact is kept from step to step in a device hash table keyed by
+     * the unordered pair: two tables of hist_cap (a power of two) entries, read *hist_parity and
+     * written the other, the roles swapping every narrow phase.  Values are the tangential
+     * displacement in the (lower id, higher id) orientation. */
+    int64_t hist_cap;
+    unsigned long long* hist_keys; /* (2, hist_cap) min id << 32 | max id, 0 = empty; zeroed before use */
+    float* hist_vals;              /* (2, hist_cap, 4) */
+    int32_t* hist_parity;          /* (1,) */
 } mwd_work;
 
 /* Scratch bytes of the deterministic accumulation for n rows and epa_cap contacts. */

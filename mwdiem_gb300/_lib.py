@@ -27,6 +27,7 @@ ST_BAD_SHAPE = 64
 ST_DEGENERATE_FACE = 128
 ST_LOG_OVERFLOW = 256
 ST_FLY_RESET = 512
+ST_HIST_OVERFLOW = 1024
 
 EPA_FACE_CAP = 128
 EPA_VERT_CAP = 32
@@ -37,7 +38,7 @@ NOALLOC_MAX_PAIRS = 1 << 18
 STATUS_NAMES = {ST_EPA_NOCONV: "EPA_NOCONV", ST_EPA_OVERFLOW: "EPA_OVERFLOW", ST_GJK_NOCONV: "GJK_NOCONV",
                 ST_PAIR_OVERFLOW: "PAIR_OVERFLOW", ST_CELL_RANGE: "CELL_RANGE", ST_CELL_CROWDED: "CELL_CROWDED",
                 ST_BAD_SHAPE: "BAD_SHAPE", ST_DEGENERATE_FACE: "DEGENERATE_FACE", ST_LOG_OVERFLOW: "LOG_OVERFLOW",
-                ST_FLY_RESET: "FLY_RESET"}
+                ST_FLY_RESET: "FLY_RESET", ST_HIST_OVERFLOW: "HIST_OVERFLOW"}
 
 
 class MwdError(RuntimeError):
@@ -89,7 +90,8 @@ class Work(C.Structure):
                 ("epa_cap", C.c_int64), ("sorted_pos", _P), ("sorted_cell", _P), ("cull_pairs", C.c_int32),
                 ("pad", C.c_int32), ("total_cells", C.c_int64),
                 ("pair_cap", C.c_int64), ("face_ids", _P), ("deterministic", C.c_int32),
-                ("pad2", C.c_int32), ("det_scratch", _P)]
+                ("pad2", C.c_int32), ("det_scratch", _P), ("hist_cap", C.c_int64), ("hist_keys", _P),
+                ("hist_vals", _P), ("hist_parity", _P)]
 
 
 DIFF_ROW = 32

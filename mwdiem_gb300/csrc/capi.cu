@@ -448,6 +448,17 @@ static int narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_wo
         a.epa_cap = work->epa_cap;
         a.pre_culled = work->cull_pairs ? 1 : 0;
         a.epa_zeroed = epa_zeroed ? 1 : 0;
+        if (work->hist_keys) {
+            if (!work->hist_vals || !work->hist_parity || work->hist_cap < 2 ||
+                (work->hist_cap & (work->hist_cap - 1))) {
+                set_error("persistent history needs hist_vals, hist_parity and a power-of-two hist_cap");
+                return MWD_ERR_INVALID;
+            }
+            a.hist_keys = work->hist_keys;
+            a.hist_vals = reinterpret_cast<float4*>(work->hist_vals);
+            a.hist_cap = work->hist_cap;
+            a.hist_parity = work->hist_parity;
+        }
         if (work->deterministic) {
             if (!work->det_scratch) {
                 set_error("deterministic accumulation needs work->det_scratch");
@@ -467,8 +478,8 @@ static int narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_wo
         }
         return launch_narrow_two_pass(a, lp | (elp << 8), reinterpret_cast<cudaStream_t>(stream));
     }
-    if (work->deterministic) {
-        set_error("deterministic accumulation needs the two-pass narrow phase (work->epa_rec)");
+    if (work->deterministic || work->hist_keys) {
+        set_error("deterministic accumulation and persistent history need the two-pass narrow phase (work->epa_rec)");
         return MWD_ERR_UNSUPPORTED;
     }
     return launch_narrow(a, 1, lp, -1, reinterpret_cast<cudaStream_t>(stream));

@@ -831,6 +831,81 @@ __global__ void __launch_bounds__(NARROW_THREADS, 6) gjk_pass_kernel(NarrowArgs 
     }
 }
 
+// ------------------------------------------------------------------ persistent tangential history
+// Open-addressing table keyed by the unordered pair (lower id << 32 | higher id; 0 = empty), linear
+// probing, the MurmurHash3 64-bit finaliser as the hash.  Values are stored in the (lower, higher)
+// orientation: a pair listed the other way round reads and writes the negated displacement.
+__device__ __forceinline__ unsigned long long hist_key(int a, int b)
+{
+    const unsigned lo = (unsigned)(a < b ? a : b), hi = (unsigned)(a < b ? b : a);
+    return ((unsigned long long)lo << 32) | hi;
+}
+__device__ __forceinline__ unsigned long long hist_hash(unsigned long long k)
+{
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+__device__ __forceinline__ f3 hist_get(const NarrowArgs& a, int A, int B)
+{
+    const int par = *a.hist_parity & 1;
+    const unsigned long long* K = a.hist_keys + (size_t)par * a.hist_cap;
+    const float4* V = a.hist_vals + (size_t)par * a.hist_cap;
+    const unsigned long long key = hist_key(A, B);
+    const unsigned long long m = (unsigned long long)a.hist_cap - 1;
+    unsigned long long slot = hist_hash(key) & m;
+    for (int64_t probe = 0; probe < a.hist_cap; ++probe) {
+        const unsigned long long k = K[slot];
+        if (k == key) {
+            const f3 v = xyz(V[slot]);
+            return A < B ? v : v * (-1.f);
+        }
+        if (k == 0ull) break;
+        slot = (slot + 1) & m;
+    }
+    return mk3(0.f, 0.f, 0.f);
+}
+__device__ __forceinline__ void hist_put(const NarrowArgs& a, int A, int B, f3 dt)
+{
+    const int par = (*a.hist_parity & 1) ^ 1;
+    unsigned long long* K = a.hist_keys + (size_t)par * a.hist_cap;
+    float4* V = a.hist_vals + (size_t)par * a.hist_cap;
+    const unsigned long long key = hist_key(A, B);
+    const unsigned long long m = (unsigned long long)a.hist_cap - 1;
+    unsigned long long slot = hist_hash(key) & m;
+    for (int64_t probe = 0; probe < a.hist_cap; ++probe) {
+        const unsigned long long prev = atomicCAS(K + slot, 0ull, key);
+        if (prev == 0ull || prev == key) {
+            V[slot] = f4(A < B ? dt : dt * (-1.f), 0.f);
+            return;
+        }
+        slot = (slot + 1) & m;
+    }
+    set_status(a.status, MWD_ST_HIST_OVERFLOW);
+}
+
+// empties the table this narrow phase writes
+__global__ void hist_clear_kernel(NarrowArgs a)
+{
+    pdl_wait();
+    pdl_launch_dependents();
+    const int par = (*a.hist_parity & 1) ^ 1;
+    unsigned long long* K = a.hist_keys + (size_t)par * a.hist_cap;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.hist_cap; i += (int64_t)gridDim.x * blockDim.x)
+        K[i] = 0ull;
+}
+
+// the table just written is read by the next narrow phase
+__global__ void hist_flip_kernel(NarrowArgs a)
+{
+    pdl_wait();
+    pdl_launch_dependents();
+    if (threadIdx.x == 0 && blockIdx.x == 0) *a.hist_parity ^= 1;
+}
+
 template <int LPP>
 __global__ void __launch_bounds__(NARROW_THREADS) epa_pass_kernel(NarrowArgs a)
 {
@@ -854,6 +929,10 @@ __global__ void __launch_bounds__(NARROW_THREADS) epa_pass_kernel(NarrowArgs a)
         const int64_t P = rec.P;
         PairView p;
         load_pair<1>(a, P, p, hA, hB, g.lane, LPP);
+        if (a.hist_keys) {
+            p.dt = hist_get(a, p.idA, p.idB);
+            p.dtn = sqrtf(p.dt.x * p.dt.x + p.dt.y * p.dt.y + p.dt.z * p.dt.z);
+        }
         g.sync();
         const mwd_material& M = a.scenes[a.st.info[p.idA] >> 1].mat[p.wall];
         Work3 wk = {0u, 0u, 0u};
@@ -871,6 +950,7 @@ __global__ void __launch_bounds__(NARROW_THREADS) epa_pass_kernel(NarrowArgs a)
                       p.IsB, fo);
         if (g.lane == 0) {
             set_status(a.status, er.status);
+            if (a.hist_keys) hist_put(a, p.idA, p.idB, fo.dt);
             if (a.det_out) {
                 float4* o = a.det_out + 3 * i;
                 o[0] = f4(fo.F, 0.f);
@@ -922,8 +1002,10 @@ int launch_two_pass_lpp(const NarrowArgs& a, cudaStream_t s)
         epa_shm_cached = shm;
     }
     if (!a.epa_zeroed) MWD_CUDA(cudaMemsetAsync(a.epa_count, 0, sizeof(int32_t), s));
+    if (a.hist_keys) MWD_CUDA(launch_pdl(hist_clear_kernel, (unsigned)(num_sms() * 4), 256, 0, s, a));
     MWD_CUDA(launch_pdl(gjk_pass_kernel<LPP>, (unsigned)(num_sms() * gjk_per_sm), NARROW_THREADS, 0, s, a));
     MWD_CUDA(launch_pdl(epa_pass_kernel<ELPP>, (unsigned)(num_sms() * epa_per_sm), NARROW_THREADS, shm, s, a));
+    if (a.hist_keys) MWD_CUDA(launch_pdl(hist_flip_kernel, 1, 32, 0, s, a));
     return MWD_OK;
 }
 

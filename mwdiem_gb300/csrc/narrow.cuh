@@ -52,6 +52,11 @@ struct NarrowArgs {
     int32_t pre_culled;     // the pair list holds only pairs whose bounding spheres overlap
     int32_t epa_zeroed;     // 1: epa_count was zeroed by an earlier kernel of the stream (the broad phase)
     float4* det_out;        // deterministic mode: (epa_cap, 3) F, TA, TB per EPA record instead of atomics
+    // persistent tangential history (two-pass mode): tables read at *hist_parity, written at the other
+    unsigned long long* hist_keys;
+    float4* hist_vals;
+    int64_t hist_cap;
+    int32_t* hist_parity;
 };
 
 int launch_narrow(const NarrowArgs& a, int mode, int lanes, int64_t n_hint, cudaStream_t s);

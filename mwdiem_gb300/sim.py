@@ -37,7 +37,7 @@ class Layout:
 
 class Simulator:
     def __init__(self, scenes, lanes=8, pair_cap=None, device="cuda", collect_collisions=False, two_pass=True,
-                 cull_pairs=True, deterministic=False):
+                 cull_pairs=True, deterministic=False, persistent_history=False):
         _dev.require_cuda()
         if isinstance(scenes, SceneSpec):
             scenes = [scenes]
@@ -49,8 +49,9 @@ class Simulator:
         self.two_pass = bool(two_pass)
         self.cull_pairs = bool(cull_pairs)
         self.deterministic = bool(deterministic)
-        if self.deterministic and not self.two_pass:
-            raise ValueError("deterministic accumulation needs the two-pass narrow phase")
+        self.persistent_history = bool(persistent_history)
+        if (self.deterministic or self.persistent_history) and not self.two_pass:
+            raise ValueError("deterministic accumulation and persistent history need the two-pass narrow phase")
         self._build_work(pair_cap, collect_collisions)
         self.graph = None
         self.graph_steps = 0
@@ -283,6 +284,15 @@ class Simulator:
         w["sorted_cell"] = torch.zeros(n, **i32)
         wk.sorted_pos = w["sorted_pos"].data_ptr()
         wk.sorted_cell = w["sorted_cell"].data_ptr()
+        if self.persistent_history:
+            hcap = 1 << max(10, int(2 * cap - 1).bit_length())  # power of two >= 2 x the contact capacity
+            w["hist_keys"] = torch.zeros(2 * hcap, dtype=torch.int64, device=self.device)
+            w["hist_vals"] = torch.zeros((2 * hcap, 4), dtype=torch.float32, device=self.device)
+            w["hist_parity"] = torch.zeros(1, **i32)
+            wk.hist_cap = hcap
+            wk.hist_keys = w["hist_keys"].data_ptr()
+            wk.hist_vals = w["hist_vals"].data_ptr()
+            wk.hist_parity = w["hist_parity"].data_ptr()
         if self.deterministic:
             nb = int(lib().mwd_det_scratch_bytes(n, cap))
             w["det_scratch"] = torch.zeros(nb, dtype=torch.uint8, device=self.device)
@@ -381,6 +391,18 @@ class Simulator:
         p = self.t["pos"][:, :3]
         v = self.t["vel"][:, :3]
         return int((~torch.isfinite(p).all(1) | ~torch.isfinite(v).all(1)).sum().item())
+
+    def history_table(self):
+        """Persistent history the next narrow phase reads: {(lower row, higher row): (3,) float32
+        tangential displacement in that orientation}."""
+        if not self.persistent_history:
+            return {}
+        cap = self.work.hist_cap
+        par = int(self.w["hist_parity"].item()) & 1
+        keys = self.w["hist_keys"][par * cap:(par + 1) * cap].cpu().numpy().view(np.uint64)
+        vals = self.w["hist_vals"][par * cap:(par + 1) * cap, :3].cpu().numpy()
+        used = np.nonzero(keys)[0]
+        return {(int(keys[i] >> np.uint64(32)), int(keys[i] & np.uint64(0xffffffff))): vals[i] for i in used}
 
     def n_pairs(self) -> int:
         return int(self.w["n_pairs"].item())

@@ -264,3 +264,46 @@ def test_settling_config1_short_horizon():
     assert dpos <= 2e-6 * size
     assert dvel <= 1e-3 * vmax
     assert dq <= 1e-4
+
+
+def test_persistent_history_matches_oracle_over_steps():
+    # the history of every pair in contact carries over to the next step (the reference drops it,
+    # MWDiem.py:953-966); checked step by step against the oracle's stride-4 history variant fed the
+    # same pair list and a host dictionary of the histories, with bit-exact (deterministic) sums
+    from mwdiem_gb300.sim import Simulator
+    sp = dense_scene(n=400, seed=21, vel=0.3)
+    sim = Simulator(sp, collect_collisions=True, cull_pairs=False, deterministic=True, persistent_history=True)
+    ref = stepper.RefStepper(sp)
+    W = sp.n_walls
+    table = {}
+    reused = 0
+    for step in range(6):
+        sim.broadphase()
+        pairs = sim.pairs().cpu().numpy()
+        inp = stepper.gather_from_sim(sim, pairs, ref.V)
+        hist = np.zeros((len(pairs), 4), np.float32)
+        for k, (a, b) in enumerate(pairs.tolist()):
+            v = table.get((min(a, b), max(a, b)))
+            if v is not None:
+                hist[k, :3] = v if a < b else -v
+                reused += 1
+        inp["hist"] = hist
+        o = oracle.contact(inp, ref.params, sim.n, "f32", hist_stride4=True, face_cap=128)
+        sim.narrow_force()
+        torch.cuda.synchronize()
+        coll = sim.w["collision"][: len(pairs)].cpu().numpy()
+        assert np.array_equal(coll, o["collision"])
+        assert np.array_equal(sim.t["force"][W:, :3].cpu().numpy(), o["force"][W:], equal_nan=True)
+        assert np.array_equal(sim.t["torque"][W:, :3].cpu().numpy(), o["torque"][W:], equal_nan=True)
+        new = {}
+        for k in np.nonzero(o["collision"] == 1)[0]:
+            a, b = int(pairs[k, 0]), int(pairs[k, 1])
+            v = o["hist"][k, :3].astype(np.float32)
+            new[(min(a, b), max(a, b))] = v if a < b else -v
+        got = sim.history_table()
+        assert set(got) == set(new)
+        for key, v in new.items():
+            assert np.array_equal(got[key], v, equal_nan=True), key
+        table = new
+        sim.integrate()
+    assert reused > 50, "contacts should carry their history across steps"
