@@ -232,6 +232,25 @@ typedef struct {
     mwd_material mat[2];    /* derived from law by mwd_derive_material (particle, wall) */
 } mwd_scene;
 
+/* Particle inlet (MWDiem.py:685-714: every few steps new hulls enter the domain).  Every row is
+ * allocated with its shape up front; rows waiting to enter carry MWD_INFO_INACTIVE in mwd_state.info
+ * and are skipped by the broad phase and the integrator.  mwd_inlet_step, run at the start of a step
+ * (mwd_step does when mwd_work.inlet is set), counts steps on the device and every `period` steps
+ * activates the next `per_spawn` rows: centre from spawn_pos, at rest, identity orientation, world
+ * vertices written.  The captured graph of a step stays valid as rows enter. */
+#define MWD_INFO_INACTIVE (1 << 30)
+typedef struct {
+    int32_t period;          /* steps between spawns (> 0) */
+    int32_t per_spawn;       /* rows activated per spawn */
+    int32_t row_end;         /* rows [*next_row, row_end) are waiting */
+    int32_t pad;
+    int32_t* next_row;       /* (1,) device: next row to activate */
+    int32_t* step;           /* (1,) device: steps seen (spawns when step % period == 0) */
+    const double* spawn_pos; /* (n,4) centre of each row when it enters (.w unused) */
+} mwd_inlet;
+
+int mwd_inlet_step(mwd_state* st, const mwd_inlet* inlet, mwd_stream_t stream);
+
 typedef struct {
     int32_t* cell_count;   /* (total_cells,) zero on entry, left zero on exit */
     int32_t* cell_start;   /* (total_cells + 1,) */
@@ -276,7 +295,9 @@ typedef struct {
     unsigned long long* hist_keys; /* (2, hist_cap) min id << 32 | max id, 0 = empty; zeroed before use */
     float* hist_vals;              /* (2, hist_cap, 4) */
     int32_t* hist_parity;          /* (1,) */
+    const mwd_inlet* inlet;        /* optional (host pointer): mwd_step runs mwd_inlet_step first */
 } mwd_work;
+
 
 /* Scratch bytes of the deterministic accumulation for n rows and epa_cap contacts. */
 int64_t mwd_det_scratch_bytes(int32_t n, int64_t epa_cap);

@@ -91,7 +91,15 @@ class Work(C.Structure):
                 ("pad", C.c_int32), ("total_cells", C.c_int64),
                 ("pair_cap", C.c_int64), ("face_ids", _P), ("deterministic", C.c_int32),
                 ("pad2", C.c_int32), ("det_scratch", _P), ("hist_cap", C.c_int64), ("hist_keys", _P),
-                ("hist_vals", _P), ("hist_parity", _P)]
+                ("hist_vals", _P), ("hist_parity", _P), ("inlet", _P)]
+
+
+INFO_INACTIVE = 1 << 30
+
+
+class Inlet(C.Structure):
+    _fields_ = [("period", C.c_int32), ("per_spawn", C.c_int32), ("row_end", C.c_int32), ("pad", C.c_int32),
+                ("next_row", _P), ("step", _P), ("spawn_pos", _P)]
 
 
 DIFF_ROW = 32
@@ -148,6 +156,7 @@ def lib():
             "mwd_contact_pairs_noalloc": (C.c_int, [i64, i32, i32] + [_P] * 20 +
                                           [C.POINTER(ContactParams), _P, _P, _P]),
             "mwd_det_scratch_bytes": (i64, [i32, i64]),
+            "mwd_inlet_step": (C.c_int, [C.POINTER(State), C.POINTER(Inlet), _P]),
             "mwd_diff_collect": (C.c_int, [C.POINTER(Diff), C.POINTER(Work), _P]),
             "mwd_diff_force": (C.c_int, [C.POINTER(Diff), _P, i32, _P]),
             "mwd_diff_integrate": (C.c_int, [C.POINTER(Diff), _P, _P, _P, C.POINTER(State), i32, _P]),
@@ -165,7 +174,7 @@ def lib():
 EXPORTED = ("mwd_last_error", "mwd_version", "mwd_num_sms", "mwd_scan_tmp_ints", "mwd_derive_material",
             "mwd_contact_pairs", "mwd_verlet_ref", "mwd_cell_keys", "mwd_wall_pairs", "mwd_linked_cell_hash",
             "mwd_broadphase", "mwd_narrow_force", "mwd_integrate", "mwd_step", "mwd_probe_fp32",
-            "mwd_contact_pairs_noalloc", "mwd_det_scratch_bytes", "mwd_diff_collect", "mwd_diff_force", "mwd_diff_integrate",
+            "mwd_contact_pairs_noalloc", "mwd_det_scratch_bytes", "mwd_inlet_step", "mwd_diff_collect", "mwd_diff_force", "mwd_diff_integrate",
             "mwd_diff_mirror", "mwd_diff_adjoint")
 
 

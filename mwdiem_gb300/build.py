@@ -21,7 +21,7 @@ LIB = BUILD / "libmwdem.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-std=c++17",
            "-Xcompiler", "-fPIC,-ffp-contract=off", "-diag-suppress", "1444", f"-I{INCLUDE}"]
-SOURCES = ["narrow.cu", "integrate.cu", "broad.cu", "capi.cu", "probe.cu", "noalloc.cu", "adjoint.cu", "reduce.cu"]
+SOURCES = ["narrow.cu", "integrate.cu", "broad.cu", "capi.cu", "probe.cu", "noalloc.cu", "adjoint.cu", "reduce.cu", "inlet.cu"]
 
 
 def nvcc() -> str:

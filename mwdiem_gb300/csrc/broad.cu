@@ -240,7 +240,11 @@ constexpr int BIG_CELL = 306;
 
 // ---------------------------------------------------------------- broad-phase kernels
 
-__device__ __forceinline__ int scene_of(const BroadArgs& a, int r) { return a.info ? (a.info[r] >> 1) : 0; }
+__device__ __forceinline__ int scene_of(const BroadArgs& a, int r)
+{
+    return a.info ? ((a.info[r] & ~MWD_INFO_INACTIVE) >> 1) : 0;
+}
+__device__ __forceinline__ bool inactive(const BroadArgs& a, int r) { return a.info && (a.info[r] & MWD_INFO_INACTIVE); }
 __device__ __forceinline__ bool is_wall(const BroadArgs& a, int r) { return a.info ? (a.info[r] & 1) : false; }
 
 struct alignas(32) dpos {
@@ -268,7 +272,7 @@ __global__ void assign_kernel(BroadArgs a)
     }
     const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= a.row_hi) return;
-    if (is_wall(a, r)) {
+    if (is_wall(a, r) || inactive(a, r)) {  // walls and rows waiting at an inlet have no cell
         a.cell_of[r] = -1;
         return;
     }

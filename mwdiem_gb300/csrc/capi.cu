@@ -498,6 +498,10 @@ int mwd_step(mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes
              int32_t lanes, int32_t n_steps, mwd_stream_t stream)
 {
     for (int i = 0; i < n_steps; ++i) {
+        if (work->inlet) {
+            int rc0 = mwd_inlet_step(st, work->inlet, stream);
+            if (rc0) return rc0;
+        }
         int rc = mwd_broadphase(st, scenes_dev, scenes_host, n_scenes, work, stream);
         if (rc) return rc;
         // the broad phase zeroed the EPA counter (assign_kernel): no memset node between the kernels

@@ -227,7 +227,7 @@ __device__ __forceinline__ void row_update(const mwd_state& st, const mwd_scene*
     const int info = st.info[P];
     dpos pos = reinterpret_cast<const dpos*>(st.pos)[P];
     float4 qacc = ld4(st.q_acc, P);
-    if (!(info & 1)) {
+    if (!(info & (1 | MWD_INFO_INACTIVE))) {  // walls and rows waiting at an inlet stay as they are
         const mwd_scene& sc = scenes[info >> 1];
         const float dt = (float)sc.dt;
         float4 Fa = ld4(st.force, P), Ta = ld4(st.torque, P);

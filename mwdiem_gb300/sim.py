@@ -15,8 +15,8 @@ import numpy as np
 import torch
 
 from . import _dev
-from ._lib import (HULL_CAP, ST_PAIR_OVERFLOW, ContactParams, Material, MwdError, Scene, State, Work, check, lib,
-                   status_names)
+from ._lib import (HULL_CAP, INFO_INACTIVE, ST_PAIR_OVERFLOW, ContactParams, Inlet, Material, MwdError, Scene, State,
+                   Work, check, lib, status_names)
 from .scene import CompactBodies, SceneSpec
 
 _STATE_F64 = ("pos", "dx_all", "wall_normal")
@@ -29,6 +29,19 @@ def _trunc(x):
 
 
 @dataclass
+class InletSpec:
+    """Particles entering during the run (MWDiem.py:685-714): the first `initial` particle rows of the
+    scene are there from the start; the others wait and enter `per_spawn` at a time every `period`
+    steps, at rest, at a point drawn uniformly (seeded) from the box `lo`..`hi`."""
+    period: int = 5
+    per_spawn: int = 1
+    initial: int = 0
+    lo: tuple = (0.0, 0.0, 0.0)
+    hi: tuple = (0.0, 0.0, 0.0)
+    seed: int = 0
+
+
+@dataclass
 class Layout:
     row_begin: list
     wall_end: list
@@ -37,7 +50,7 @@ class Layout:
 
 class Simulator:
     def __init__(self, scenes, lanes=8, pair_cap=None, device="cuda", collect_collisions=False, two_pass=True,
-                 cull_pairs=True, deterministic=False, persistent_history=False):
+                 cull_pairs=True, deterministic=False, persistent_history=False, inlet=None):
         _dev.require_cuda()
         if isinstance(scenes, SceneSpec):
             scenes = [scenes]
@@ -53,6 +66,9 @@ class Simulator:
         if (self.deterministic or self.persistent_history) and not self.two_pass:
             raise ValueError("deterministic accumulation and persistent history need the two-pass narrow phase")
         self._build_work(pair_cap, collect_collisions)
+        self.inlet = None
+        if inlet is not None:
+            self._build_inlet(inlet)
         self.graph = None
         self.graph_steps = 0
         self.steps_done = 0
@@ -302,6 +318,37 @@ class Simulator:
         wk.pair_cap = cap
         self.work = wk
         self.pair_cap = cap
+
+    def _build_inlet(self, spec: InletSpec):
+        if len(self.specs) != 1:
+            raise ValueError("the inlet is for a single scene")
+        if spec.period < 1 or spec.per_spawn < 0:
+            raise ValueError("inlet period must be >= 1 and per_spawn >= 0")
+        w0, r1 = self.layout.wall_end[0], self.layout.row_end[0]
+        first = w0 + int(spec.initial)
+        if first > r1:
+            raise ValueError("more initial particles than the scene has")
+        rng = np.random.default_rng(spec.seed)
+        sp = np.zeros((self.n, 4))
+        lo, hi = np.asarray(spec.lo, float), np.asarray(spec.hi, float)
+        sp[first:r1, :3] = lo + rng.random((r1 - first, 3)) * (hi - lo)
+        dev = self.device
+        info = self.t["info"]
+        info[first:r1] = info[first:r1] | INFO_INACTIVE
+        self.inlet_t = {"spawn_pos": torch.from_numpy(sp).to(dev),
+                        "next_row": torch.tensor([first], dtype=torch.int32, device=dev),
+                        "step": torch.zeros(1, dtype=torch.int32, device=dev)}
+        st = Inlet()
+        st.period, st.per_spawn, st.row_end = int(spec.period), int(spec.per_spawn), int(r1)
+        st.next_row = self.inlet_t["next_row"].data_ptr()
+        st.step = self.inlet_t["step"].data_ptr()
+        st.spawn_pos = self.inlet_t["spawn_pos"].data_ptr()
+        self.inlet = st
+        self.work.inlet = C.addressof(st)
+
+    def active_rows(self):
+        """Boolean (n,) mask of the rows in the domain (walls included)."""
+        return (self.t["info"] & INFO_INACTIVE) == 0
 
     # ------------------------------------------------------------------ stepping
     def step(self, n_steps=1, stream=None):

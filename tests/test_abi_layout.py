@@ -18,6 +18,7 @@ STRUCTS = {
     "mwd_work": "Work",
     "mwd_contact_rec": "ContactRec",
     "mwd_diff": "Diff",
+    "mwd_inlet": "Inlet",
 }
 
 

@@ -307,3 +307,36 @@ def test_persistent_history_matches_oracle_over_steps():
         table = new
         sim.integrate()
     assert reused > 50, "contacts should carry their history across steps"
+
+
+def test_inlet_rows_enter_on_schedule():
+    # particles entering during the run (MWDiem.py:685-714): rows wait outside the broad phase and the
+    # integrator and enter per_spawn at a time every period steps, also inside a captured graph
+    from mwdiem_gb300.sim import InletSpec, Simulator
+    sp = dense_scene(n=300, seed=31, vel=0.0)
+    inl = InletSpec(period=5, per_spawn=2, initial=200, lo=(-5.0, -5.0, 15.5), hi=(5.0, 5.0, 17.5), seed=1)
+    W = sp.n_walls
+    eager = Simulator(sp, inlet=inl)
+    assert int(eager.active_rows()[W:].sum()) == 200
+    waiting0 = ~eager.active_rows().cpu().numpy()
+    start = eager.t["pos"].cpu().numpy().copy()
+    eager.step(30)
+    torch.cuda.synchronize()
+    act = eager.active_rows().cpu().numpy()
+    assert act[W:].sum() == 200 + 2 * 6          # spawns at steps 0, 5, ..., 25
+    entered = np.nonzero(act & waiting0)[0]
+    assert np.array_equal(entered, np.arange(W + 200, W + 212))
+    pos = eager.t["pos"].cpu().numpy()
+    spawn = eager.inlet_t["spawn_pos"].cpu().numpy()
+    assert np.all(np.abs(pos[entered, :2] - spawn[entered, :2]) < 0.05)   # at rest, falling
+    assert np.all(pos[entered, 2] <= spawn[entered, 2]) and np.all(pos[entered, 2] > 15.0)
+    still = np.nonzero(~act)[0]
+    assert np.array_equal(pos[still], start[still])                        # waiting rows untouched
+    pairs = eager.pairs().cpu().numpy()
+    assert not np.isin(pairs, still).any()
+    graph = Simulator(sp, inlet=inl)
+    graph.capture(1)                              # one eager step, then replays of the captured step
+    graph.replay(29)
+    torch.cuda.synchronize()
+    assert np.array_equal(graph.active_rows().cpu().numpy(), act)
+    assert np.abs(graph.t["pos"].cpu().numpy()[act] - pos[act]).max() <= 1e-6 * 16.0
