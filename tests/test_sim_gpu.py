@@ -328,8 +328,9 @@ def test_inlet_rows_enter_on_schedule():
     assert np.array_equal(entered, np.arange(W + 200, W + 212))
     pos = eager.t["pos"].cpu().numpy()
     spawn = eager.inlet_t["spawn_pos"].cpu().numpy()
-    assert np.all(np.abs(pos[entered, :2] - spawn[entered, :2]) < 0.05)   # at rest, falling
-    assert np.all(pos[entered, 2] <= spawn[entered, 2]) and np.all(pos[entered, 2] > 15.0)
+    # entered at rest at the spawn points (two entering together may overlap and push each other)
+    assert np.all(np.abs(pos[entered, :3] - spawn[entered, :3]) < 0.05)
+    assert np.all(pos[entered, 2] > 15.0)
     still = np.nonzero(~act)[0]
     assert np.array_equal(pos[still], start[still])                        # waiting rows untouched
     pairs = eager.pairs().cpu().numpy()
