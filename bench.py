@@ -36,6 +36,9 @@ WORKLOAD = ("pour20k: 20,000 convex hulls of U{12..32} points on a sphere of rad
             "ratio 0.3 (en=et=0.372), mu 0.5, dt 5e-5")
 METRIC = "particle-steps/s"
 WINDOW_STEPS = 500  # the pour configuration runs 500 steps
+# DRAM bytes (read + write) of one GJK-pass and one EPA-pass launch of this step, from the ncu capture
+# summarised in profiles/step_kernels_pour20k.md (5.205 MB + 0.151 MB; writes stay in L2)
+NARROW_DRAM_BYTES_PER_LAUNCH = 5.204992e6 + 0.151040e6
 KERNELS_PER_STEP = 11  # broad phase 7 (assign, 2 scan, scatter, order, crowded, append) + GJK pass + EPA pass + integrate rows + vertices
 
 
@@ -357,7 +360,11 @@ def breakdown(sim, V, flush, reps=10):
     if dom == "narrow":
         a = flops / (ms["narrow"] * 1e-3) / 1e12
         roof = {"kernel": "gjk_pass_kernel + epa_pass_kernel", "bound": "fp32", "achieved": a, "peak": fp32_peak,
-                "unit": "TFLOP/s", "frac": a / fp32_peak if fp32_peak else None, "traffic": None,
+                "unit": "TFLOP/s", "frac": a / fp32_peak if fp32_peak else None,
+                "traffic": NARROW_DRAM_BYTES_PER_LAUNCH,
+                "traffic_source": "profiles/step_kernels_pour20k.md (ncu dram__bytes_read + write, one launch each)",
+                "note": "latency-bound: ~13k candidate pairs, each a chain of dependent support queries; the "
+                        "GJK pass issues on ~44% of cycles, the EPA pass waits on its few longest pairs",
                 "peak_source": "measured in this run (mwd_probe_fp32: FMUL+FADD chains, no FMA)"}
     elif dom == "integrate":
         hbm = pk.get("hbm_gbs", 6800.0)
@@ -428,7 +435,10 @@ def pairs_rate(n_pairs, lanes, reps=5, with_cpu=True):
     ps = PairScene(n_pairs, seed=1, lanes=lanes)
     stream = torch.cuda.current_stream()
     sweep = {}
-    for cand in (8 | (8 << 8), 8 | (16 << 8), 8 | (32 << 8), 4 | (16 << 8), 16 | (16 << 8)):
+    cands = (8 | (8 << 8), 8 | (16 << 8), 4 | (16 << 8), 16 | (16 << 8), 4 | (16 << 8) | (1 << 16),
+             4 | (8 << 8) | (1 << 16), 8 | (16 << 8) | (1 << 16), 1 | (16 << 8), 1 | (16 << 8) | (1 << 16),
+             1 | (8 << 8) | (1 << 16))
+    for cand in cands:
         ps.lanes = cand
         ps.narrow()
         torch.cuda.synchronize()
@@ -441,8 +451,7 @@ def pairs_rate(n_pairs, lanes, reps=5, with_cpu=True):
         sweep[autotune.describe(cand)] = e0.elapsed_time(e1) / reps
     best = min(sweep, key=sweep.get)
     ms = sweep[best]
-    ps.lanes = [c for c in (8 | (8 << 8), 8 | (16 << 8), 8 | (32 << 8), 4 | (16 << 8), 16 | (16 << 8))
-                if autotune.describe(c) == best][0]
+    ps.lanes = [c for c in cands if autotune.describe(c) == best][0]
     ps.narrow(count_work=True)
     torch.cuda.synchronize()
     dots, faces, queries = (int(x) for x in ps.w["counters"].cpu().numpy())

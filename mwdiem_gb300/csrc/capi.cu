@@ -428,10 +428,14 @@ static int narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_wo
         return MWD_ERR_UNSUPPORTED;
     }
     int lp;
-    int rc = check_lanes(lanes & 0xff, &lp);
+    // the GJK pass of the two-pass narrow phase also runs one lane per pair
+    const bool gjk_one = (lanes & 0xff) == 1 && work->epa_rec;
+    int rc = gjk_one ? MWD_OK : check_lanes(lanes & 0xff, &lp);
     if (rc) return rc;
+    if (gjk_one) lp = 1;
     const int elp = (lanes >> 8) & 0xff;
     NarrowArgs a = {};
+    a.epa_global = (lanes >> 16) & 1;
     a.st = *st;
     a.scenes = scenes_dev;
     a.pairs = work->pairs;

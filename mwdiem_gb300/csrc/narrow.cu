@@ -75,6 +75,7 @@ __device__ __forceinline__ unsigned fkey(float f)
 template <int LPP>
 __device__ __forceinline__ int group_argmax(const Group<LPP>& g, float v, int i)
 {
+    if (LPP == 1) return i;  // one lane per pair: its own scan is the sequential one
     const unsigned k = fkey(v);
     const unsigned km = __reduce_max_sync(g.mask, k);
     return (int)__reduce_min_sync(g.mask, k == km ? (unsigned)i : 0xffffffffu);
@@ -428,7 +429,7 @@ struct PairView {
 
 template <int MODE>
 __device__ __forceinline__ bool load_pair(const NarrowArgs& a, int64_t P, PairView& p, float4* hA, float4* hB,
-                                          int lane, int lpp)
+                                          int lane, int lpp, bool stage = true)
 {
     if (MODE == 0) {
         const float* c;
@@ -476,9 +477,11 @@ __device__ __forceinline__ bool load_pair(const NarrowArgs& a, int64_t P, PairVi
         p.nA = a.st.vert_off[p.idA + 1] - oa;
         p.nB = a.st.vert_off[p.idB + 1] - ob;
         if (p.nA > a.hull_cap || p.nB > a.hull_cap) return false;
-        const float4* wv = reinterpret_cast<const float4*>(a.st.world_verts);
-        for (int i = lane; i < p.nA; i += lpp) hA[i] = wv[oa + i];
-        for (int i = lane; i < p.nB; i += lpp) hB[i] = wv[ob + i];
+        if (stage) {
+            const float4* wv = reinterpret_cast<const float4*>(a.st.world_verts);
+            for (int i = lane; i < p.nA; i += lpp) hA[i] = wv[oa + i];
+            for (int i = lane; i < p.nB; i += lpp) hB[i] = wv[ob + i];
+        }
     }
     p.dtn = sqrtf(p.dt.x * p.dt.x + p.dt.y * p.dt.y + p.dt.z * p.dt.z);
     return true;
@@ -919,8 +922,7 @@ __global__ void __launch_bounds__(NARROW_THREADS) epa_pass_kernel(NarrowArgs a)
     g.mask = LPP == 32 ? 0xffffffffu : (((1u << LPP) - 1u) << ((threadIdx.x & 31) / LPP * LPP));
     EpaMem* em = reinterpret_cast<EpaMem*>(smem) + grp;
     float4* hull = reinterpret_cast<float4*>(reinterpret_cast<EpaMem*>(smem) + GPB) + (size_t)grp * 2 * a.hull_cap;
-    float4* hA = hull;
-    float4* hB = hull + a.hull_cap;
+    const float4* wv = reinterpret_cast<const float4*>(a.st.world_verts);
     const int cnt = *a.epa_count;
     const int64_t m = cnt < a.epa_cap ? cnt : a.epa_cap;
     const SimplexRec* recs = reinterpret_cast<const SimplexRec*>(a.epa_rec);
@@ -928,7 +930,14 @@ __global__ void __launch_bounds__(NARROW_THREADS) epa_pass_kernel(NarrowArgs a)
         const SimplexRec rec = recs[i];
         const int64_t P = rec.P;
         PairView p;
-        load_pair<1>(a, P, p, hA, hB, g.lane, LPP);
+        // the hulls staged in shared memory, or read in place from the (L1-cached) vertex table
+        const float4* hA = hull;
+        const float4* hB = hull + a.hull_cap;
+        load_pair<1>(a, P, p, hull, hull + a.hull_cap, g.lane, LPP, !a.epa_global);
+        if (a.epa_global) {
+            hA = wv + a.st.vert_off[p.idA];
+            hB = wv + a.st.vert_off[p.idB];
+        }
         if (a.hist_keys) {
             p.dt = hist_get(a, p.idA, p.idB);
             p.dtn = sqrtf(p.dt.x * p.dt.x + p.dt.y * p.dt.y + p.dt.z * p.dt.z);
@@ -990,7 +999,7 @@ int launch_two_pass_lpp(const NarrowArgs& a, cudaStream_t s)
         MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, gjk_pass_kernel<LPP>, NARROW_THREADS, 0));
         gjk_per_sm = v < 1 ? 1 : v;
     }
-    const size_t shm = (size_t)GPB * sizeof(EpaMem) + (size_t)GPB * 2 * a.hull_cap * sizeof(float4);
+    const size_t shm = (size_t)GPB * sizeof(EpaMem) + (a.epa_global ? 0 : (size_t)GPB * 2 * a.hull_cap * sizeof(float4));
     if (!attr) {
         MWD_CUDA(cudaFuncSetAttribute(epa_pass_kernel<ELPP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         attr = true;
@@ -1090,12 +1099,13 @@ int launch_narrow_two_pass(const NarrowArgs& a, int lanes, cudaStream_t s)
     int el = (lanes >> 8) & 0xff;
     if (!el) el = gl;
 #define MWD_TP(G, E) if (gl == G && el == E) return launch_two_pass_lpp<G, E>(a, s)
+    MWD_TP(1, 4); MWD_TP(1, 8); MWD_TP(1, 16); MWD_TP(1, 32);
     MWD_TP(4, 4); MWD_TP(4, 8); MWD_TP(4, 16); MWD_TP(4, 32);
     MWD_TP(8, 8); MWD_TP(8, 16); MWD_TP(8, 32); MWD_TP(8, 4);
     MWD_TP(16, 16); MWD_TP(16, 32); MWD_TP(16, 8); MWD_TP(16, 4);
     MWD_TP(32, 32); MWD_TP(32, 16); MWD_TP(32, 8); MWD_TP(32, 4);
 #undef MWD_TP
-    set_error("lanes per pair must be 4, 8, 16 or 32 (got GJK %d, EPA %d)", gl, el);
+    set_error("lanes per pair must be 1 (GJK pass only), 4, 8, 16 or 32 (got GJK %d, EPA %d)", gl, el);
     return MWD_ERR_INVALID;
 }
 

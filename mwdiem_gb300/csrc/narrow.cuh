@@ -52,6 +52,8 @@ struct NarrowArgs {
     int32_t pre_culled;     // the pair list holds only pairs whose bounding spheres overlap
     int32_t epa_zeroed;     // 1: epa_count was zeroed by an earlier kernel of the stream (the broad phase)
     float4* det_out;        // deterministic mode: (epa_cap, 3) F, TA, TB per EPA record instead of atomics
+    int32_t epa_global;     // 1: the EPA pass reads the hulls from global memory (L1) instead of staging them
+    int32_t pad3;
     // persistent tangential history (two-pass mode): tables read at *hist_parity, written at the other
     unsigned long long* hist_keys;
     float4* hist_vals;
