@@ -65,7 +65,22 @@ typedef struct {
     int32_t hist_mode; /* 0: the reference's stride-1 history indexing (.cu:974-976); 1: stride 4 */
     int32_t lanes;     /* lanes per pair in the narrow phase: 4, 8, 16, 32; 0 = default (8) */
     int32_t deterministic; /* 1: per-particle sums in pair order instead of float atomics */
+    int32_t law;       /* MWD_LAW_REFERENCE (the reference's law as written) or MWD_LAW_PHYSICAL */
+    int32_t pad;
 } mwd_contact_params;
+
+/* Contact laws.  MWD_LAW_REFERENCE reproduces .cu:647-871 as written: mu stands in for the effective
+ * mass in tc, Gn, Kt and Gt, and the contact point is (cpA - cpB) / 2, which puts the torque arm near
+ * -c_A.  MWD_LAW_PHYSICAL (device-resident step only) is the same linear spring-dashpot law with
+ *   m_n = 1 / (1/m_A + 1/m_B)                         normal effective mass (a wall's 1/m is 0)
+ *   m_t = 1 / (1/m_A + 1/m_B + dA^2/I_A + dB^2/I_B)   tangential effective mass (a wall adds no term)
+ *   tc = sqrt(m_n (pi^2 + ln^2 en) / Kn),  Gn = -2 m_n ln en / tc
+ *   Kt = m_t (pi^2 + ln^2 et) / tc^2,      Gt = -2 m_t ln et / tc
+ * and the contact point (cpA + cpB) / 2, so a normal impact of two bodies rebounds with restitution
+ * en whatever their masses; mu is only the Coulomb coefficient.  I is the inertia size (trace / 3),
+ * as in the reference's tangential term. */
+#define MWD_LAW_REFERENCE 0
+#define MWD_LAW_PHYSICAL 1
 
 /* Per-material constants of the contact law that do not depend on the pair, derived once on the
  * host from mwd_contact_params with the same float/double operand types the reference uses
@@ -78,10 +93,14 @@ typedef struct {
     float Gn;     /* normal damping */
     float ln_et;  /* logf((float)et) */
     float dt_f;   /* (float)dt */
-    float pad[3];
+    float ln_en;  /* logf((float)en) */
+    float Xn;     /* pi^2 + ln^2 en (float) */
+    float Xt;     /* pi^2 + ln^2 et (float) */
     double mu;    /* mu as a double (Coulomb test is done in double, .cu:774) */
     double inv_mu;
     double KtA;
+    int32_t physical; /* MWD_LAW_PHYSICAL: tc, Gn, Kt, Gt per pair from the masses (see above) */
+    int32_t pad;
 } mwd_material;
 
 /* Fills m[0] (particle-particle) and m[1] (particle-wall) from prm (host pointers). */

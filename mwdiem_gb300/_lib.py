@@ -51,13 +51,19 @@ class ContactParams(C.Structure):
     _fields_ = [("Kn", C.c_double), ("en", C.c_double), ("et", C.c_double), ("mu", C.c_double),
                 ("Kn_wall", C.c_double), ("en_wall", C.c_double), ("et_wall", C.c_double),
                 ("mu_wall", C.c_double), ("dt", C.c_double), ("n_wall", C.c_int32),
-                ("hist_mode", C.c_int32), ("lanes", C.c_int32), ("deterministic", C.c_int32)]
+                ("hist_mode", C.c_int32), ("lanes", C.c_int32), ("deterministic", C.c_int32),
+                ("law", C.c_int32), ("pad", C.c_int32)]
+
+
+LAW_REFERENCE = 0
+LAW_PHYSICAL = 1
 
 
 class Material(C.Structure):
     _fields_ = [("Kn_f", C.c_float), ("mu_f", C.c_float), ("Gn", C.c_float), ("ln_et", C.c_float),
-                ("dt_f", C.c_float), ("pad", C.c_float * 3), ("mu", C.c_double), ("inv_mu", C.c_double),
-                ("KtA", C.c_double)]
+                ("dt_f", C.c_float), ("ln_en", C.c_float), ("Xn", C.c_float), ("Xt", C.c_float),
+                ("mu", C.c_double), ("inv_mu", C.c_double), ("KtA", C.c_double), ("physical", C.c_int32),
+                ("pad", C.c_int32)]
 
 
 class VerletParams(C.Structure):

@@ -107,7 +107,7 @@ int check_lanes(int lanes, int* out)
 // Pair-independent constants, with the reference's operand types (gpu_fine_contact_detection.cu:685-701):
 // log of a float argument in float, pi^2 + ln^2 in float, the products with the double literals
 // mu and Kn in double.  Evaluated on the host with the C library's logf, like the oracle.
-static void derive_one(double Kn, double en, double et, double mu, double dt, mwd_material* m)
+static void derive_one(double Kn, double en, double et, double mu, double dt, int32_t law, mwd_material* m)
 {
     const float pii = (float)3.141592653589793;
     const float Len = logf((float)en), Let = logf((float)et);
@@ -119,10 +119,14 @@ static void derive_one(double Kn, double en, double et, double mu, double dt, mw
     m->Gn = (float)((-1) * 2 * mu / (double)tc * (double)Len);
     m->ln_et = Let;
     m->dt_f = (float)dt;
-    m->pad[0] = m->pad[1] = m->pad[2] = 0.f;
+    m->ln_en = Len;
+    m->Xn = Xen;
+    m->Xt = Xet;
     m->mu = mu;
     m->inv_mu = 1 / mu;
     m->KtA = Kn * (double)Xet / (double)Xen;
+    m->physical = law == MWD_LAW_PHYSICAL ? 1 : 0;
+    m->pad = 0;
 }
 
 }  // namespace mwd
@@ -156,8 +160,12 @@ int mwd_derive_material(const mwd_contact_params* prm, mwd_material m[2])
         set_error("mwd_derive_material: null argument");
         return MWD_ERR_INVALID;
     }
-    derive_one(prm->Kn, prm->en, prm->et, prm->mu, prm->dt, &m[0]);
-    derive_one(prm->Kn_wall, prm->en_wall, prm->et_wall, prm->mu_wall, prm->dt, &m[1]);
+    if (prm->law != MWD_LAW_REFERENCE && prm->law != MWD_LAW_PHYSICAL) {
+        set_error("mwd_derive_material: unknown contact law %d", prm->law);
+        return MWD_ERR_INVALID;
+    }
+    derive_one(prm->Kn, prm->en, prm->et, prm->mu, prm->dt, prm->law, &m[0]);
+    derive_one(prm->Kn_wall, prm->en_wall, prm->et_wall, prm->mu_wall, prm->dt, prm->law, &m[1]);
     return MWD_OK;
 }
 
@@ -184,6 +192,10 @@ int mwd_contact_pairs(int64_t n_pairs, int32_t V, int32_t n_particles, const flo
     }
     if (prm->deterministic) {
         set_error("deterministic accumulation is not available for the per-pair layout");
+        return MWD_ERR_UNSUPPORTED;
+    }
+    if (prm->law != MWD_LAW_REFERENCE) {
+        set_error("the per-pair layout carries no masses: only the reference contact law is available");
         return MWD_ERR_UNSUPPORTED;
     }
     int lanes;

@@ -265,8 +265,9 @@ __device__ __forceinline__ void row_update(const mwd_state& st, const mwd_scene*
         wbf = whbf + alpha * (dt * 0.5f);
         w = qtrip(q, wbf, qconj(q));
         f3 v = vh + F * (invm * dt);
-        // vertices compound the rotation q every step (gpu_Verlet.cu:279-305): q_acc <- q q_acc
-        qacc = qmul(q, qacc);
+        // vertices compound the rotation q every step (gpu_Verlet.cu:279-305): q_acc <- q q_acc;
+        // under the physical law the vertices follow the orientation itself: q_acc <- q
+        qacc = sc.mat[0].physical ? q : qmul(q, qacc);
         float qn = rsqrtf(qacc.x * qacc.x + qacc.y * qacc.y + qacc.z * qacc.z + qacc.w * qacc.w);
         qacc = make_float4(qacc.x * qn, qacc.y * qn, qacc.z * qn, qacc.w * qn);
         dpos np;

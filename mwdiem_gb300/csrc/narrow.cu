@@ -376,17 +376,40 @@ struct ForceResult {
 };
 
 // Force (.cu:647-871) with the pair-independent constants taken from mwd_material
+// imA, imB: inverse masses (0 for a wall side), read only by the physical law.
 __device__ __forceinline__ void contact_force(f3 cA, f3 cB, float depth, f3 n, f3 cpA, f3 cpB, const mwd_material& M,
                                               f3 vA, f3 vB, f3 wA, f3 wB, f3 dt, float4 qA, float dtn, float IsA,
-                                              float IsB, ForceResult& o)
+                                              float IsB, float imA, float imB, ForceResult& o)
 {
-    f3 cp = (cpA - cpB) / 2.f;
-    f3 dA = cp - cA, dB = cp - cB;
-    float dA2 = dA.x * dA.x + dA.y * dA.y + dA.z * dA.z;
-    float dB2 = dB.x * dB.x + dB.y * dB.y + dB.z * dB.z;
-    double C = M.inv_mu + (double)(dA2 / IsA) + (double)(dB2 / IsB);
-    float Kt = (float)(M.KtA * 1 / C);
-    float Gt = (float)((-1) * 2 / C * (double)M.ln_et);
+    f3 cp;
+    float Kt, Gt, Gn;
+    if (!M.physical) {
+        cp = (cpA - cpB) / 2.f;
+        f3 dA = cp - cA, dB = cp - cB;
+        float dA2 = dA.x * dA.x + dA.y * dA.y + dA.z * dA.z;
+        float dB2 = dB.x * dB.x + dB.y * dB.y + dB.z * dB.z;
+        double C = M.inv_mu + (double)(dA2 / IsA) + (double)(dB2 / IsB);
+        Kt = (float)(M.KtA * 1 / C);
+        Gt = (float)((-1) * 2 / C * (double)M.ln_et);
+        Gn = M.Gn;
+    } else {
+        // effective masses from the pair; tc and the dampings follow from them (MWD_LAW_PHYSICAL)
+        cp = (cpA + cpB) / 2.f;
+        f3 dA = cp - cA, dB = cp - cB;
+        float dA2 = dA.x * dA.x + dA.y * dA.y + dA.z * dA.z;
+        float dB2 = dB.x * dB.x + dB.y * dB.y + dB.z * dB.z;
+        const float im = imA + imB;
+        const float mn = 1.f / im;
+        const float tc2 = mn * M.Xn / M.Kn_f;
+        const float tc = sqrtf(tc2);
+        Gn = (-2.f) * mn * M.ln_en / tc;
+        float C = im;
+        if (imA != 0.f) C = C + dA2 / IsA;
+        if (imB != 0.f) C = C + dB2 / IsB;
+        const float mt = 1.f / C;
+        Kt = mt * M.Xt / tc2;
+        Gt = (-2.f) * mt * M.ln_et / tc;
+    }
     if (dot(cB - cA, n) < 0.f) n = n * (-1.f);
     float nn = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
     n = n / nn;
@@ -398,7 +421,7 @@ __device__ __forceinline__ void contact_force(f3 cA, f3 cB, float depth, f3 n, f
     f3 tij = mk3(0.f, 0.f, 0.f);
     if (utn != 0.f) tij = ut / utn;
     if (utn == 0.f && dtn != 0.f) tij = dt / dtn;
-    f3 Fn = (disp_n * (-1.f)) * M.Kn_f - un * M.Gn;
+    f3 Fn = (disp_n * (-1.f)) * M.Kn_f - un * Gn;
     float Fnn = sqrtf(Fn.x * Fn.x + Fn.y * Fn.y + Fn.z * Fn.z);
     f3 Ft = dt * (-1.f) * Kt - ut * Gt;
     float Ftn = sqrtf(Ft.x * Ft.x + Ft.y * Ft.y + Ft.z * Ft.z);
@@ -485,6 +508,20 @@ __device__ __forceinline__ bool load_pair(const NarrowArgs& a, int64_t P, PairVi
     }
     p.dtn = sqrtf(p.dt.x * p.dt.x + p.dt.y * p.dt.y + p.dt.z * p.dt.z);
     return true;
+}
+
+// Inverse masses of a pair's two rows for the physical law (0 for a wall row); the per-pair layout
+// (MODE 0) carries no masses and only runs the reference law.
+template <int MODE>
+__device__ __forceinline__ void pair_inv_mass(const NarrowArgs& a, const PairView& p, const mwd_material& M,
+                                              float& imA, float& imB)
+{
+    imA = 0.f;
+    imB = 0.f;
+    if (MODE == 0 || !M.physical) return;
+    const float4* ii = reinterpret_cast<const float4*>(a.st.inv_inertia);
+    if (!(a.st.info[p.idA] & 1)) imA = ii[p.idA].w;
+    if (!(a.st.info[p.idB] & 1)) imB = ii[p.idB].w;
 }
 
 template <int MODE>
@@ -602,8 +639,10 @@ __device__ void process_pair(const NarrowArgs& a, int64_t P, const Group<LPP>& g
                     support<LPP>(g, hA, p.nA, hB, p.nB, d4, S4, a4, b4, wk);
                 }
                 epa<LPP>(g, em, hA, p.nA, hB, p.nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er, wk);
+                float imA, imB;
+                pair_inv_mass<MODE>(a, p, M, imA, imB);
                 contact_force(p.cA, p.cB, er.depth, er.n, er.cpA, er.cpB, M, p.vA, p.vB, p.wA, p.wB, p.dt, p.qA,
-                              p.dtn, p.IsA, p.IsB, fo);
+                              p.dtn, p.IsA, p.IsB, imA, imB, fo);
                 st |= er.status;
                 resolved = true;
                 break;
@@ -955,8 +994,10 @@ __global__ void __launch_bounds__(NARROW_THREADS) epa_pass_kernel(NarrowArgs a)
         EpaResult er;
         epa<LPP>(g, *em, hA, p.nA, hB, p.nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er, wk);
         ForceResult fo;
+        float imA, imB;
+        pair_inv_mass<1>(a, p, M, imA, imB);
         contact_force(p.cA, p.cB, er.depth, er.n, er.cpA, er.cpB, M, p.vA, p.vB, p.wA, p.wB, p.dt, p.qA, p.dtn, p.IsA,
-                      p.IsB, fo);
+                      p.IsB, imA, imB, fo);
         if (g.lane == 0) {
             set_status(a.status, er.status);
             if (a.hist_keys) hist_put(a, p.idA, p.idB, fo.dt);

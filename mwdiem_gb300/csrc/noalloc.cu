@@ -91,6 +91,10 @@ extern "C" int mwd_contact_pairs_noalloc(int64_t n_pairs, int32_t V, int32_t n_p
         set_error("deterministic accumulation is not available for the per-pair layout");
         return MWD_ERR_UNSUPPORTED;
     }
+    if (prm->law != MWD_LAW_REFERENCE) {
+        set_error("the per-pair layout carries no masses: only the reference contact law is available");
+        return MWD_ERR_UNSUPPORTED;
+    }
     int lanes = prm->lanes ? prm->lanes : 8;
     if (lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32) {
         set_error("lanes per pair must be 4, 8, 16 or 32 (got %d)", lanes);

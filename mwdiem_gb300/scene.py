@@ -75,6 +75,7 @@ class SceneSpec:
     gravity: tuple = (0.0, 0.0, -G)
     max_particlesize: float = 2.4
     name: str = "scene"
+    law: str = "reference"   # contact law: "reference" (as the reference computes it) or "physical"
 
     @property
     def n_walls(self) -> int:
@@ -86,6 +87,33 @@ class SceneSpec:
 
     def body_list(self):
         return self.bodies.expand() if isinstance(self.bodies, CompactBodies) else list(self.bodies)
+
+    def principal_bodies(self):
+        """The particles re-expressed in the principal axes of their inertia, as the physical contact
+        law integrates them: (bodies, q0) where bodies holds the same shapes with body-frame vertices
+        r_p along the principal axes and diagonal moments, and q0 (n_particles, 4) is each particle's
+        starting orientation, R(q0) r_p = its world-oriented vertices.  (The reference keeps the
+        world-oriented vertices as the body frame and takes the eigenvalues of the inertia tensor as
+        body-frame moments, Particle_class.py:125-156, which is exact only for shapes whose principal
+        axes lie along x, y, z.)"""
+        cb = self.bodies
+        if isinstance(cb, CompactBodies):
+            pool, qp = [], []
+            for b in cb.pool:
+                r, lam, q = shapes.principal_frame(b.vertices, b.mass)
+                pool.append(Body(vertices=r, inertia_bf=lam, inertia_size=b.inertia_size, mass=b.mass))
+                qp.append(q)
+            pick = np.asarray(cb.pick, dtype=np.int64)
+            quats = np.asarray(cb.quats, dtype=np.float64)
+            q0 = np.array([shapes.quat_mul(quats[k], qp[pick[k]]) for k in range(len(pick))]).reshape(-1, 4)
+            ident = np.tile([1.0, 0.0, 0.0, 0.0], (len(pick), 1))
+            return CompactBodies(pool=pool, pick=pick, quats=ident), q0
+        out, q0 = [], []
+        for b in cb:
+            r, lam, q = shapes.principal_frame(b.vertices, b.mass)
+            out.append(Body(vertices=r, inertia_bf=lam, inertia_size=b.inertia_size, mass=b.mass))
+            q0.append(q)
+        return out, np.array(q0).reshape(-1, 4)
 
     def wall_bbox(self):
         lo = np.full(3, np.inf)

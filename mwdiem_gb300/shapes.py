@@ -136,6 +136,62 @@ def quat_to_matrix(q):
                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
 
 
+def matrix_to_quat(R):
+    """Unit quaternion (w, x, y, z), w >= 0, of a rotation matrix (Shepperd's method: the largest of
+    the four squared components comes from the trace or a diagonal entry, the others from the
+    off-diagonal sums and differences)."""
+    R = np.asarray(R, dtype=np.float64)
+    t = np.trace(R)
+    k = int(np.argmax([t, R[0, 0], R[1, 1], R[2, 2]]))
+    if k == 0:
+        w = 0.5 * np.sqrt(1.0 + t)
+        s = 0.25 / w
+        q = [w, (R[2, 1] - R[1, 2]) * s, (R[0, 2] - R[2, 0]) * s, (R[1, 0] - R[0, 1]) * s]
+    elif k == 1:
+        x = 0.5 * np.sqrt(1.0 + R[0, 0] - R[1, 1] - R[2, 2])
+        s = 0.25 / x
+        q = [(R[2, 1] - R[1, 2]) * s, x, (R[0, 1] + R[1, 0]) * s, (R[0, 2] + R[2, 0]) * s]
+    elif k == 2:
+        y = 0.5 * np.sqrt(1.0 - R[0, 0] + R[1, 1] - R[2, 2])
+        s = 0.25 / y
+        q = [(R[0, 2] - R[2, 0]) * s, (R[0, 1] + R[1, 0]) * s, y, (R[1, 2] + R[2, 1]) * s]
+    else:
+        z = 0.5 * np.sqrt(1.0 - R[0, 0] - R[1, 1] + R[2, 2])
+        s = 0.25 / z
+        q = [(R[1, 0] - R[0, 1]) * s, (R[0, 2] + R[2, 0]) * s, (R[1, 2] + R[2, 1]) * s, z]
+    q = np.asarray(q)
+    q = q / np.sqrt(q @ q)
+    return q if q[0] >= 0 else -q
+
+
+def quat_mul(a, b):
+    """Hamilton product a b of quaternions (w, x, y, z): R(a b) = R(a) R(b)."""
+    aw, av = a[0], np.asarray(a[1:])
+    bw, bv = b[0], np.asarray(b[1:])
+    v = aw * bv + bw * av + np.cross(av, bv)
+    return np.concatenate([[aw * bw - av @ bv], v])
+
+
+def hull_inertia(vertices, mass):
+    """Inertia tensor, about the origin of ``vertices`` (the body centre), of their convex hull
+    carrying ``mass`` uniformly (the closed form of ``inertia_tensor``)."""
+    from scipy.spatial import ConvexHull
+    v = np.asarray(vertices, dtype=np.float64)
+    h = ConvexHull(v)
+    faces, normals = _outward_faces(v, h.simplices, v[h.vertices].mean(axis=0))
+    return inertia_tensor(v, faces, normals, mass / h.volume)
+
+
+def principal_frame(vertices, mass):
+    """(r_p, moments, q0): the vertices expressed in the principal axes of the hull's inertia, the
+    principal moments, and the orientation q0 with R(q0) r_p = vertices."""
+    I = hull_inertia(vertices, mass)
+    lam, P = np.linalg.eigh(I)
+    if np.linalg.det(P) < 0:
+        P[:, 2] = -P[:, 2]
+    return np.ascontiguousarray(np.asarray(vertices, dtype=np.float64) @ P), lam, matrix_to_quat(P)
+
+
 def random_quaternion(rng):
     q = rng.normal(size=4)
     return q / np.sqrt(q @ q)

@@ -15,9 +15,11 @@ import numpy as np
 import torch
 
 from . import _dev
-from ._lib import (HULL_CAP, INFO_INACTIVE, ST_PAIR_OVERFLOW, ContactParams, Inlet, Material, MwdError, Scene, State,
-                   Work, check, lib, status_names)
+from ._lib import (HULL_CAP, INFO_INACTIVE, LAW_PHYSICAL, LAW_REFERENCE, ST_PAIR_OVERFLOW, ContactParams, Inlet,
+                   Material, MwdError, Scene, State, Work, check, lib, status_names)
 from .scene import CompactBodies, SceneSpec
+
+CONTACT_LAWS = {"reference": LAW_REFERENCE, "physical": LAW_PHYSICAL}
 
 _STATE_F64 = ("pos", "dx_all", "wall_normal")
 _STATE_F32 = ("vel", "vel_half", "w_half_bf", "w_bf", "w", "q", "q_half", "q_all", "q_acc", "force", "torque",
@@ -98,6 +100,9 @@ class Simulator:
             for k, (b, _, _) in enumerate(sp.walls):
                 explicit.append((row + k, b.vertices))
             cb = sp.bodies
+            q0 = np.tile([1.0, 0.0, 0.0, 0.0], (n_p, 1))
+            if sp.law == "physical":  # principal-axes body frames (SceneSpec.principal_bodies)
+                cb, q0 = sp.principal_bodies()
             if isinstance(cb, CompactBodies):
                 key = id(cb.pool)
                 if key not in pools:
@@ -130,7 +135,8 @@ class Simulator:
                 mass=np.concatenate([wall_mass, p_mass]),
                 ext=np.concatenate([np.zeros((W, 3)), p_mass[:, None] * g[None, :]]),
                 info=np.concatenate([np.full(W, (s_id << 1) | 1), np.full(n_p, s_id << 1)]).astype(np.int32),
-                cnt=np.concatenate([wall_cnt, p_cnt]), rad=np.concatenate([wall_rad, p_rad])))
+                cnt=np.concatenate([wall_cnt, p_cnt]), rad=np.concatenate([wall_rad, p_rad]),
+                q0=np.concatenate([np.tile([1.0, 0.0, 0.0, 0.0], (W, 1)), q0])))
             row += W
             we.append(row)
             row += n_p
@@ -199,8 +205,10 @@ class Simulator:
             t[k] = z4.clone()
         qid = torch.zeros((n, 4), **f32)
         qid[:, 0] = 1.0
-        for k in ("q", "q_half", "q_all", "q_acc"):
-            t[k] = qid.clone()
+        t["q_all"] = qid
+        q0 = torch.from_numpy(cat["q0"].astype(np.float32)).to(dev)  # identity unless a principal frame
+        for k in ("q", "q_half", "q_acc"):
+            t[k] = q0.clone()
         ext4 = np.zeros((n, 4), np.float32)
         ext4[:, :3] = cat["ext"]
         t["ext_force"] = torch.from_numpy(ext4).to(dev)
@@ -212,6 +220,16 @@ class Simulator:
         owner = torch.repeat_interleave(torch.arange(n, device=dev), counts_d)
         world = body.clone()
         world[:, :3] = (t["pos"][owner, :3] + body[:, :3].double()).float()
+        turned = torch.from_numpy(np.nonzero(np.any(cat["q0"] != [1.0, 0.0, 0.0, 0.0], axis=1))[0]).to(dev)
+        if len(turned):  # principal-axes rows start at q0: world = pos + R(q0) r_p
+            sel = torch.isin(owner, turned).nonzero().squeeze(1)
+            q0d = torch.from_numpy(cat["q0"]).to(dev)
+            chunk = 1 << 20
+            for a0 in range(0, len(sel), chunk):
+                vi = sel[a0:a0 + chunk]
+                R = _quat_to_matrix(q0d[owner[vi]])
+                rot = torch.einsum("vij,vj->vi", R, body[vi, :3].double())
+                world[vi, :3] = (t["pos"][owner[vi], :3] + rot).float()
         t["world_verts"] = world
         # the integrator's vertex pass: one thread per vertex, through each row's transform
         t["vert_owner"] = owner.to(torch.int32)
@@ -254,6 +272,9 @@ class Simulator:
             sc.law = ContactParams(float(sp.Kn), float(sp.en), float(sp.et), float(sp.mu), float(sp.Kn_wall),
                                    float(sp.en_wall), float(sp.et_wall), float(sp.mu_wall), float(sp.dt),
                                    int(sp.n_walls), 0, self.lanes, 0)
+            if sp.law not in CONTACT_LAWS:
+                raise ValueError(f"unknown contact law {sp.law!r}; expected one of {sorted(CONTACT_LAWS)}")
+            sc.law.law = CONTACT_LAWS[sp.law]
             check(lib().mwd_derive_material(C.byref(sc.law), sc.mat))
         self.scenes_host = arr
         self.total_cells = base

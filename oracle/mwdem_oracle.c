@@ -38,7 +38,7 @@ typedef struct {
     int n_wall;
     int hist_stride4; /* 0: reference stride-1 history indexing, 1: stride 4 */
     int face_cap;     /* EPA face-list capacity (<= ORC_FCAP); 0 -> ORC_FCAP */
-    int pad;
+    int physical;     /* 1: the physical-mass contact law (effective masses, midpoint contact point) */
 } orc_contact_params;
 
 /* ---------------- narrow phase, FP32 ---------------- */
@@ -105,7 +105,8 @@ static d3 matvec_d(const double* M, d3 v)
 typedef struct {
     double dt;
     double box[6]; /* xmax, xmin, ymax, ymin, zmax, zmin */
-    int n_min, n_max, V, pad;
+    int n_min, n_max, V;
+    int physical; /* 1: rotate the vertices by this step's rotation q_new q_old^-1 instead of by q */
 } orc_verlet_params;
 
 /* Arrays in the reference's layout (MWDiem.py:603-631): v, v12, w12bf, wbf, w, F, T, com, dxall
@@ -167,9 +168,18 @@ int orc_verlet_f64(int N, double* v, double* v12, double* w12bf, double* q12, do
         om = qtrip_d(qq, ombf, qqi);
         vel = d3add(vel12, d3div(d3mul(f, dt), m));
         double* vp = verts + (size_t)P * V * 3;
+        double qr[4], qri[4];
+        if (prm->physical) {  /* the vertices follow the orientation: rotate by q_new q_old^-1 */
+            double qoi[4];
+            qinv_d(qold, qoi);
+            qmul_d(qq, qoi, qr);
+        } else {              /* the reference rotates them by the whole orientation q every step */
+            for (int i = 0; i < 4; ++i) qr[i] = qq[i];
+        }
+        qinv_d(qr, qri);
         for (int i = 0; i < V; ++i) {
             d3 r = d3sub(d3ld(vp + 3 * i), c);
-            d3st(vp + 3 * i, d3add(qtrip_d(qq, r, qqi), c));
+            d3st(vp + 3 * i, d3add(qtrip_d(qr, r, qri), c));
         }
         c = d3add(c, dx);
         for (int i = 0; i < V; ++i) d3st(vp + 3 * i, d3add(d3ld(vp + 3 * i), dx));

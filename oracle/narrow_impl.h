@@ -324,25 +324,51 @@ typedef struct { V3 F, TA, TB; } ORC_N(force_out);
 
 /* Linear spring-dashpot normal force, tangential spring-dashpot with a Coulomb cap, torques
  * (gpu_fine_contact_detection.cu:647-871).  mu doubles as the effective mass and as the friction
- * coefficient, as in the reference.  dt (the history) is updated in place. */
+ * coefficient, as in the reference.  dt (the history) is updated in place.
+ *
+ * prm->physical selects the physical-mass variant of the same law (not in the reference): normal
+ * effective mass mn = 1/(imA + imB), tangential mt = 1/(imA + imB + dA^2/IsA + dB^2/IsB) (a wall
+ * side, im = 0, adds no term), tc = sqrt(mn (pi^2 + ln^2 en)/Kn), Gn = -2 mn ln en / tc,
+ * Kt = mt (pi^2 + ln^2 et)/tc^2, Gt = -2 mt ln et / tc, contact point (cpA + cpB)/2. */
 static void ORC_N(force)(V3 cA, V3 cB, RT depth, V3 n, V3 cpA, V3 cpB, const orc_contact_params* prm,
                          V3 vA, V3 vB, V3 wA, V3 wB, V3* dt, const RT* qA, RT dtn, RT IsA, RT IsB,
-                         int wall, ORC_N(force_out)* o)
+                         int wall, RT imA, RT imB, ORC_N(force_out)* o)
 {
     double Kn = wall ? prm->Kn_wall : prm->Kn;
     double mu = wall ? prm->mu_wall : prm->mu;
     RT en = (RT)(wall ? prm->en_wall : prm->en);
     RT et = (RT)(wall ? prm->et_wall : prm->et);
-    V3 cp = ORC_N(div)(ORC_N(sub)(cpA, cpB), (RT)2);
-    V3 dA = ORC_N(sub)(cp, cA), dB = ORC_N(sub)(cp, cB);
-    RT dA2 = dA.x * dA.x + dA.y * dA.y + dA.z * dA.z;
-    RT dB2 = dB.x * dB.x + dB.y * dB.y + dB.z * dB.z;
     RT pii = (RT)3.141592653589793;
     RT Len = ORC_LOG(en), Let = ORC_LOG(et);
-    RT tc = ORC_SQRT_D(mu * (pii * pii + Len * Len) / Kn);
-    RT Gn = (-1) * 2 * mu / tc * Len;
-    RT Kt = Kn * (pii * pii + Let * Let) / (pii * pii + Len * Len) * 1 / (1 / mu + dA2 / IsA + dB2 / IsB);
-    RT Gt = (-1) * 2 / (1 / mu + dA2 / IsA + dB2 / IsB) * Let;
+    V3 cp;
+    RT Gn, Kt, Gt;
+    if (!prm->physical) {
+        cp = ORC_N(div)(ORC_N(sub)(cpA, cpB), (RT)2);
+        V3 dA = ORC_N(sub)(cp, cA), dB = ORC_N(sub)(cp, cB);
+        RT dA2 = dA.x * dA.x + dA.y * dA.y + dA.z * dA.z;
+        RT dB2 = dB.x * dB.x + dB.y * dB.y + dB.z * dB.z;
+        RT tc = ORC_SQRT_D(mu * (pii * pii + Len * Len) / Kn);
+        Gn = (-1) * 2 * mu / tc * Len;
+        Kt = Kn * (pii * pii + Let * Let) / (pii * pii + Len * Len) * 1 / (1 / mu + dA2 / IsA + dB2 / IsB);
+        Gt = (-1) * 2 / (1 / mu + dA2 / IsA + dB2 / IsB) * Let;
+    } else {
+        cp = ORC_N(div)(ORC_N(add)(cpA, cpB), (RT)2);
+        V3 dA = ORC_N(sub)(cp, cA), dB = ORC_N(sub)(cp, cB);
+        RT dA2 = dA.x * dA.x + dA.y * dA.y + dA.z * dA.z;
+        RT dB2 = dB.x * dB.x + dB.y * dB.y + dB.z * dB.z;
+        RT Xn = pii * pii + Len * Len, Xt = pii * pii + Let * Let;
+        RT im = imA + imB;
+        RT mn = (RT)1 / im;
+        RT tc2 = mn * Xn / (RT)Kn;
+        RT tc = ORC_SQRT(tc2);
+        Gn = (RT)-2 * mn * Len / tc;
+        RT Cm = im;
+        if (imA != 0) Cm = Cm + dA2 / IsA;
+        if (imB != 0) Cm = Cm + dB2 / IsB;
+        RT mt = (RT)1 / Cm;
+        Kt = mt * Xt / tc2;
+        Gt = (RT)-2 * mt * Let / tc;
+    }
     if (ORC_N(dot)(ORC_N(sub)(cB, cA), n) < 0.0) n = ORC_N(mul)(n, (RT)-1.0);
     RT nn = ORC_SQRT(n.x * n.x + n.y * n.y + n.z * n.z);
     n = ORC_N(div)(n, nn);
@@ -383,7 +409,8 @@ void ORC_N(orc_contact)(int npairs, int V, const RT* Acom, const RT* Bcom, const
                         const RT* Avel, const RT* Bvel, const RT* Aw, const RT* Bw, const int* Anv,
                         const int* Bnv, const int* Aid, const int* Bid, RT* hist, RT* force, RT* torque,
                         const RT* qA, const RT* qB, const RT* IsA, const RT* IsB, int* collision,
-                        const orc_contact_params* prm, RT* diag, int* status, int* counters)
+                        const orc_contact_params* prm, RT* diag, int* status, int* counters, const RT* imA,
+                        const RT* imB)
 {
     int stride4 = prm->hist_stride4;
     int fcap = (prm->face_cap > 4 && prm->face_cap < ORC_FCAP) ? prm->face_cap : ORC_FCAP;
@@ -462,7 +489,7 @@ void ORC_N(orc_contact)(int npairs, int V, const RT* Acom, const RT* Bcom, const
                     ORC_N(epa)(S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, HA, HB, &eo, &nsup, fcap);
                     ORC_N(force_out) fo;
                     ORC_N(force)(cA, cB, eo.depth, eo.normal, eo.cpA, eo.cpB, prm, vA, vB, wA, wB, &dt, qa,
-                                 dtn, IA, IB, wall, &fo);
+                                 dtn, IA, IB, wall, imA ? imA[P] : (RT)0, imB ? imB[P] : (RT)0, &fo);
                     F = fo.F; TA = fo.TA; TB = fo.TB;
                     st |= eo.status;
                     resolved = 1;

@@ -33,12 +33,12 @@ class ContactParams(C.Structure):
     _fields_ = [("Kn", C.c_double), ("en", C.c_double), ("et", C.c_double), ("mu", C.c_double),
                 ("Kn_wall", C.c_double), ("en_wall", C.c_double), ("et_wall", C.c_double),
                 ("mu_wall", C.c_double), ("dt", C.c_double), ("n_wall", C.c_int),
-                ("hist_stride4", C.c_int), ("face_cap", C.c_int), ("pad", C.c_int)]
+                ("hist_stride4", C.c_int), ("face_cap", C.c_int), ("physical", C.c_int)]
 
 
 class VerletParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("box", C.c_double * 6), ("n_min", C.c_int), ("n_max", C.c_int),
-                ("V", C.c_int), ("pad", C.c_int)]
+                ("V", C.c_int), ("physical", C.c_int)]
 
 
 _lib = None
@@ -52,7 +52,7 @@ def lib():
         for name in ("orc_contact_f32", "orc_contact_f64"):
             f = getattr(_lib, name)
             f.restype = None
-            f.argtypes = [C.c_int, C.c_int] + [P] * 20 + [C.POINTER(ContactParams), P, P, P]
+            f.argtypes = [C.c_int, C.c_int] + [P] * 20 + [C.POINTER(ContactParams), P, P, P, P, P]
         _lib.orc_verlet_f64.restype = C.c_int
         _lib.orc_verlet_f64.argtypes = [C.c_int] + [P] * 16 + [C.POINTER(VerletParams)]
         _lib.orc_cell_keys.restype = None
@@ -79,18 +79,20 @@ CONTACT_INPUTS = ("A_com", "B_com", "A_verts", "B_verts", "A_vel", "B_vel", "A_a
                   "A_nv", "B_nv", "A_id", "B_id", "hist", "qA", "qB", "IsA", "IsB")
 
 
-def contact_params(p: dict, hist_stride4=False, face_cap=0) -> ContactParams:
+def contact_params(p: dict, hist_stride4=False, face_cap=0, physical=False) -> ContactParams:
     return ContactParams(float(p["Kn"]), float(p["en"]), float(p["et"]), float(p["mu"]),
                          float(p["Kn_wall"]), float(p["en_wall"]), float(p["et_wall"]), float(p["mu_wall"]),
                          float(p["timestep"]), int(p["num_particles_wall"]), int(bool(hist_stride4)),
-                         int(face_cap), 0)
+                         int(face_cap), int(bool(physical)))
 
 
 def contact(inp: dict, params: dict, n_particles: int, precision="f32", force=None, torque=None,
-            hist_stride4=False, face_cap=0):
+            hist_stride4=False, face_cap=0, inv_mass=None):
     """Run the oracle narrow phase + force over per-pair arrays.
 
     ``inp`` holds the arrays named in ``CONTACT_INPUTS`` (shapes as in ``MWDiem.py:887-903``).
+    ``inv_mass=(imA, imB)``, per-pair inverse masses (0 for a wall side), selects the physical-mass
+    contact law instead of the reference's.
     Returns a dict with force, torque (n_particles,3), hist (P,4), collision (P,), diag (P,19),
     status (P,), counters (P,9).
     """
@@ -105,13 +107,16 @@ def contact(inp: dict, params: dict, n_particles: int, precision="f32", force=No
     diag = np.zeros((n, DIAG), dt)
     status = np.zeros(n, np.int32)
     counters = np.zeros((n, NCOUNT), np.int32)
-    prm = contact_params(params, hist_stride4, face_cap)
+    prm = contact_params(params, hist_stride4, face_cap, physical=inv_mass is not None)
+    imA = imB = None
+    if inv_mass is not None:
+        imA, imB = (_c(x, dt) for x in inv_mass)
     fn = lib().orc_contact_f32 if precision == "f32" else lib().orc_contact_f64
     if n:
         fn(n, V, _p(a["A_com"]), _p(a["B_com"]), _p(a["A_verts"]), _p(a["B_verts"]), _p(a["A_vel"]),
            _p(a["B_vel"]), _p(a["A_angvel"]), _p(a["B_angvel"]), _p(a["A_nv"]), _p(a["B_nv"]),
            _p(a["A_id"]), _p(a["B_id"]), _p(hist), _p(F), _p(T), _p(a["qA"]), _p(a["qB"]), _p(a["IsA"]),
-           _p(a["IsB"]), _p(coll), C.byref(prm), _p(diag), _p(status), _p(counters))
+           _p(a["IsB"]), _p(coll), C.byref(prm), _p(diag), _p(status), _p(counters), _p(imA), _p(imB))
     return dict(force=F, torque=T, hist=hist, collision=coll, diag=diag, status=status, counters=counters)
 
 
@@ -119,23 +124,26 @@ VERLET_ARRAYS = ("v", "v12", "w12bf", "q12", "q", "qall", "wbf", "w", "F", "T", 
                  "Iinv", "I", "dxall")
 
 
-def verlet_params(dt, box, n_min, n_max, V) -> VerletParams:
+def verlet_params(dt, box, n_min, n_max, V, physical=False) -> VerletParams:
     vp = VerletParams()
     vp.dt = float(dt)
     for i in range(6):
         vp.box[i] = float(box[i])
     vp.n_min, vp.n_max, vp.V = int(n_min), int(n_max), int(V)
+    vp.physical = int(bool(physical))
     return vp
 
 
-def verlet_f64(state: dict, dt, box, n_min, n_max) -> int:
-    """One FP64 integrator step in place over reference-layout arrays; returns resets."""
+def verlet_f64(state: dict, dt, box, n_min, n_max, physical=False) -> int:
+    """One FP64 integrator step in place over reference-layout arrays; returns resets.
+    ``physical``: the vertices turn by the step's rotation (the physical contact law's integrator)
+    instead of by the whole orientation as in the reference."""
     for k in VERLET_ARRAYS:
         a = state[k]
         assert a.dtype == np.float64 and a.flags.c_contiguous, k
     N = state["v"].shape[0]
     V = state["verts"].shape[1]
-    prm = verlet_params(dt, box, n_min, n_max, V)
+    prm = verlet_params(dt, box, n_min, n_max, V, physical)
     return lib().orc_verlet_f64(N, *[_p(state[k]) for k in VERLET_ARRAYS], C.byref(prm))
 
 

@@ -17,13 +17,25 @@ from __future__ import annotations
 import numpy as np
 
 import oracle
+from mwdiem_gb300.shapes import quat_to_matrix
 
 
 class RefStepper:
     def __init__(self, spec, V=None, kind="port", nthreads=1):
         """spec: mwdiem_gb300.scene.SceneSpec (walls first, then particles)."""
         W = spec.n_walls
-        bodies = [b for b, _, _ in spec.walls] + spec.body_list()
+        self.law = getattr(spec, "law", "reference")
+        q0 = np.tile([1.0, 0.0, 0.0, 0.0], (W + spec.n_particles, 1))
+        if self.law == "physical":
+            # principal-axes body frames and starting orientations (SceneSpec.principal_bodies)
+            pb, q0[W:] = spec.principal_bodies()
+            parts = pb.expand() if hasattr(pb, "expand") else pb
+            rot = [quat_to_matrix(q) for q in q0[W:]]
+            parts = [type(b)(vertices=b.vertices @ R.T, inertia_bf=b.inertia_bf, inertia_size=b.inertia_size,
+                             mass=b.mass) for b, R in zip(parts, rot)]
+        else:
+            parts = spec.body_list()
+        bodies = [b for b, _, _ in spec.walls] + parts
         centres = np.concatenate([np.array([c for _, c, _ in spec.walls]).reshape(-1, 3), spec.centres], 0)
         N = len(bodies)
         nv = np.array([b.vertices.shape[0] for b in bodies], dtype=np.int32)
@@ -41,7 +53,7 @@ class RefStepper:
         z = lambda: np.zeros((N, 3))  # noqa: E731
         q = lambda: np.tile([1.0, 0.0, 0.0, 0.0], (N, 1))  # noqa: E731
         st = dict(v=z(), v12=z(), w12bf=z(), wbf=z(), w=z(), F=z(), T=z(), com=centres.copy(), dxall=z(),
-                  q12=q(), q=q(), qall=q(), verts=verts, mass=mass, Iinv=Iinv, I=I)
+                  q12=q0.copy(), q=q0.copy(), qall=q(), verts=verts, mass=mass, Iinv=Iinv, I=I)
         if spec.velocities is not None:
             st["v"][W:] = spec.velocities
             st["v12"][W:] = spec.velocities
@@ -64,6 +76,8 @@ class RefStepper:
                            num_particles_wall=W, timestep=spec.dt)
         self.kind = kind
         self.nthreads = nthreads
+        if self.law != "reference" and kind == "reference":
+            raise ValueError("the reference's own kernel has only its own contact law")
         if kind == "reference":
             self.ref_c = oracle.RefContact(self.params, "f32")
             vp = dict(timestep_size=spec.dt, num_particles=N, num_vertices_max=V, syssize_x_max=self.box[0],
@@ -101,6 +115,12 @@ class RefStepper:
                     hist=np.zeros((P, 4), f32), qA=st["q"][a].astype(f32), qB=st["q"][b].astype(f32),
                     IsA=self.Is[a].astype(f32), IsB=self.Is[b].astype(f32))
 
+    def inv_mass(self, pairs):
+        """Per-pair inverse masses (float32, 0 for a wall side) for the physical contact law."""
+        im = (1.0 / self.st["mass"]).astype(np.float32)
+        im[: self.W] = 0.0
+        return im[pairs[:, 0]], im[pairs[:, 1]]
+
     def step(self):
         st, W, N = self.st, self.W, self.N
         pairs = self.candidate_pairs()
@@ -110,7 +130,8 @@ class RefStepper:
             if self.kind == "reference":
                 r = self.ref_c.run(inp, N, nthreads=self.nthreads, snapshot=True)
             else:
-                r = oracle.contact(inp, self.params, N, "f32")
+                r = oracle.contact(inp, self.params, N, "f32",
+                                   inv_mass=self.inv_mass(pairs) if self.law == "physical" else None)
             force, torque = r["force"], r["torque"]
             self.last_collision = r["collision"]
         else:
@@ -123,8 +144,15 @@ class RefStepper:
         if self.kind == "reference":
             self.ref_v.run(st, nthreads=self.nthreads)
         else:
-            oracle.verlet_f64(st, self.dt, self.box, W, N)
+            oracle.verlet_f64(st, self.dt, self.box, W, N, physical=self.law == "physical")
         return len(pairs)
+
+
+def inv_mass_from_sim(sim, pairs):
+    """Per-pair inverse masses (0 for a wall row) as the device step reads them."""
+    im = sim.t["inv_inertia"][:, 3].cpu().numpy().copy()
+    im[(sim.t["info"].cpu().numpy() & 1) != 0] = 0.0
+    return im[pairs[:, 0]], im[pairs[:, 1]]
 
 
 def gather_from_sim(sim, pairs, V):

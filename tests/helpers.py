@@ -3,6 +3,7 @@ from __future__ import annotations
 
 import numpy as np
 
+from mwdiem_gb300 import scene as scene_mod
 from mwdiem_gb300 import shapes
 
 CONTACT_PARAMS = dict(Kn=1e5, en=0.372, et=0.372, mu=0.5, Kn_wall=1e5, en_wall=0.372, et_wall=0.372,
@@ -111,3 +112,22 @@ def make_verlet_state(N, V, seed, W=3, box=5.0, dt=1e-3):
     st["v12"][W + 1] = [1e4, 0, 0]
     bx = (box, -box, box, -box, box, -box)
     return st, bx
+
+
+def head_on_cubes(law, density=4.0, v=0.5):
+    """Two unit cubes (mass 4) meeting head-on along x at relative speed 2v, no gravity, in a 10 x 10
+    box."""
+    # cube A turned so that a body diagonal points along +x, its corner hitting the face of the
+    # axis-aligned cube B: a corner-face contact whose normal and contact point lie (almost) on the
+    # line of centres, so the impact is normal and nearly torque-free (a face-face contact from one
+    # contact point would tip the cubes)
+    axis = np.array([0.0, 1.0, -1.0]) / np.sqrt(2.0)
+    th = np.arccos(1.0 / np.sqrt(3.0))
+    q = np.concatenate([[np.cos(th / 2)], np.sin(th / 2) * axis])
+    A = scene_mod.body_from_shape(shapes.cube(1.0, density), q)
+    B = scene_mod.body_from_shape(shapes.cube(1.0, density))
+    walls = scene_mod.box_walls(10.0, 10.0, 10.0, 2.0)
+    centres = np.array([[-0.01 - np.sqrt(3.0) / 2, 0.0, 5.0], [0.51, 0.02, 5.013]])
+    return scene_mod.SceneSpec(walls=walls, bodies=[A, B], centres=centres,
+                               velocities=np.array([[v, 0.0, 0.0], [-v, 0.0, 0.0]]), gravity=(0.0, 0.0, 0.0),
+                               max_particlesize=float(2 * shapes.cube(1.0).radius), law=law)

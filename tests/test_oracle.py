@@ -58,6 +58,42 @@ def test_contact_golden_history_variants():
         assert bits_equal(o1[k], z[f"stride1_{k}"]), k
 
 
+def test_physical_law_closed_form():
+    # the physical-mass variant of the contact law (not in the reference) on a known answer: two
+    # axis-aligned cubes overlapping by 0.1 along x, A approaching at 0.2, masses 4 and 2.  The normal
+    # force is Kn depth + Gn u_n with Gn = -2 m_n ln en / tc, tc = sqrt(m_n (pi^2 + ln^2 en) / Kn),
+    # m_n = 1 / (1/4 + 1/2); no tangential motion, so no tangential force; torques about the
+    # midpoint contact point (cpA + cpB) / 2.
+    from helpers import cube_pair_kat
+    params = dict(CONTACT_PARAMS, num_particles_wall=0)
+    inp = {k: np.asarray(v, np.float64) if np.asarray(v).dtype == np.float32 else v
+           for k, v in cube_pair_kat(depth=0.1).items()}
+    inp["A_vel"] = np.array([[0.2, 0.0, 0.0]])
+    imA, imB = np.array([0.25]), np.array([0.5])
+    o = oracle.contact(inp, params, 2, "f64", inv_mass=(imA, imB))
+    assert o["collision"][0] == 1
+    d = o["diag"][0]
+    depth = d[0]  # 0.1 up to the float32 rounding of the fixture's vertices
+    assert abs(depth - 0.1) < 1e-6
+    mn = 1.0 / (0.25 + 0.5)
+    Len = np.log(params["en"])
+    tc = np.sqrt(mn * (np.pi ** 2 + Len ** 2) / params["Kn"])
+    Gn = -2.0 * mn * Len / tc
+    F = np.array([-(params["Kn"] * depth + Gn * 0.2), 0.0, 0.0])
+    assert np.allclose(o["force"][0], F, rtol=1e-12, atol=1e-9)
+    assert np.allclose(o["force"][1], -F, rtol=1e-12, atol=1e-9)
+    cp = (d[4:7] + d[7:10]) / 2
+    assert np.allclose(o["torque"][0], np.cross(cp - inp["A_com"][0], F), rtol=1e-9, atol=1e-9)
+    assert np.allclose(o["torque"][1], np.cross(cp - inp["B_com"][0], -F), rtol=1e-9, atol=1e-9)
+    # the reference's law on the same pair uses mu = 0.5 as the mass: a different damping force
+    r = oracle.contact(inp, params, 2, "f64")
+    assert abs(r["force"][0, 0] - F[0]) > 1.0
+    # FP32 restatement of the physical law against the FP64 one
+    o32 = oracle.contact(cube_pair_kat(depth=0.1) | {"A_vel": np.array([[0.2, 0.0, 0.0]], np.float32)}, params, 2,
+                         "f32", inv_mass=(imA, imB))
+    assert np.allclose(o32["force"], o["force"], rtol=1e-5, atol=1e-2)
+
+
 def test_verlet_golden():
     z = np.load(G / "verlet.npz")
     st = {k[3:]: z[k].copy() for k in z.files if k.startswith("in_")}

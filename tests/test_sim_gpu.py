@@ -15,6 +15,7 @@ import torch
 
 import oracle
 import stepper
+from helpers import head_on_cubes
 from mwdiem_gb300 import scene
 
 pytestmark = pytest.mark.gpu
@@ -307,6 +308,75 @@ def test_persistent_history_matches_oracle_over_steps():
         table = new
         sim.integrate()
     assert reused > 50, "contacts should carry their history across steps"
+
+
+def test_physical_law_sums_equal_oracle():
+    # the physical-mass contact law (effective masses, midpoint contact point): per-particle sums in
+    # pair-list order, bit-identical to the oracle's serial loop running the same law
+    from mwdiem_gb300.sim import Simulator
+    sp = dense_scene(n=600, seed=17)
+    sp.law = "physical"
+    sim = Simulator(sp, collect_collisions=True, cull_pairs=False, deterministic=True)
+    sim.broadphase()
+    pairs = sim.pairs().cpu().numpy()
+    sim.narrow_force()
+    torch.cuda.synchronize()
+    ref = stepper.RefStepper(sp)
+    o = oracle.contact(stepper.gather_from_sim(sim, pairs, ref.V), ref.params, sim.n, "f32", face_cap=128,
+                       inv_mass=stepper.inv_mass_from_sim(sim, pairs))
+    coll = sim.w["collision"][: len(pairs)].cpu().numpy()
+    assert np.array_equal(coll, o["collision"]) and (coll == 1).sum() > 100
+    W = sp.n_walls
+    assert np.array_equal(sim.t["force"][W:, :3].cpu().numpy(), o["force"][W:], equal_nan=True)
+    assert np.array_equal(sim.t["torque"][W:, :3].cpu().numpy(), o["torque"][W:], equal_nan=True)
+    sim.check_status()
+
+
+@pytest.mark.parametrize("kind,steps", [("dense", 20), ("gentle", 100)])
+def test_physical_law_short_horizon(kind, steps):
+    # the physical law against the FP64 reference path running the same law (principal-axes body
+    # frames, vertices turned by each step's rotation), same scenes and bars as the reference law
+    from mwdiem_gb300.sim import Simulator
+    sp = dense_scene(n=400, seed=3) if kind == "dense" else dense_scene(n=400, seed=3, spacing=2.45, vel=0.05)
+    sp.law = "physical"
+    sim = Simulator(sp, collect_collisions=True)
+    ref = stepper.RefStepper(sp)
+    for _ in range(steps):
+        ref.step()
+    sim.step(steps)
+    torch.cuda.synchronize()
+    W = sp.n_walls
+    g = sim.reference_state()
+    dpos = np.abs(g["com"][W:] - ref.st["com"][W:]).max()
+    vmax = np.abs(ref.st["v"][W:]).max()
+    dvel = np.abs(g["v"][W:] - ref.st["v"][W:]).max()
+    dq = np.abs(g["q"][W:] - ref.st["q"][W:]).max()
+    print(f"physical law, {kind} {steps} steps: |dpos| {dpos:.3e} |dv| {dvel:.3e} (vmax {vmax:.3e}) |dq| {dq:.3e}")
+    assert (ref.last_collision == 1).sum() > 5
+    assert dpos <= 2e-6 * 16.0
+    assert dvel <= 1e-3 * vmax
+    assert dq <= 1e-4
+    sim.check_status()
+
+
+def test_physical_law_restitution():
+    # a normal impact of two cubes of mass 4 rebounds with the restitution en of the law; the
+    # reference's law, which uses mu = 0.5 as the effective mass (the true one is 2), damps it less
+    # (and its contact point (cpA - cpB) / 2 spins the cubes)
+    from mwdiem_gb300.sim import Simulator
+    got = {}
+    for law in ("physical", "reference"):
+        sp = head_on_cubes(law)
+        sim = Simulator(sp)
+        sim.step(1500)  # contact starts after ~400 steps and lasts ~300 (tc = 0.0147 s, dt 5e-5)
+        torch.cuda.synchronize()
+        W = sp.n_walls
+        v = sim.t["vel"][W:W + 2, :3].cpu().numpy()
+        got[law] = -(v[0, 0] - v[1, 0]) / 1.0
+    print("restitution:", got, "en", head_on_cubes("physical").en)
+    en = head_on_cubes("physical").en
+    assert abs(got["physical"] - en) < 0.02
+    assert abs(got["reference"] - en) > 0.1
 
 
 def test_inlet_rows_enter_on_schedule():
