@@ -34,6 +34,25 @@ SCENE = dict(n=N_PARTICLES, seed=0, box=40.0, spacing=2.6, jitter=0.1, n_min=12,
 WORKLOAD = ("pour20k: 20,000 convex hulls of U{12..32} points on a sphere of radius U[0.8,1.2], jittered "
             "lattice (spacing 2.6) in a 40x40 box, random orientations, at rest, gravity; kn 1e5, damping "
             "ratio 0.3 (en=et=0.372), mu 0.5, dt 5e-5")
+class host_prints_to_stderr:
+    """The reference's kernels report some cases with printf (e.g. "No min depth found!",
+    gpu_fine_contact_detection.cu:437); while they run on the host their C-level stdout goes to
+    stderr, so that stdout carries only this script's JSON line."""
+
+    def __enter__(self):
+        sys.stdout.flush()
+        self.saved = os.dup(1)
+        os.dup2(2, 1)
+        return self
+
+    def __exit__(self, *exc):
+        import ctypes
+        ctypes.CDLL(None).fflush(None)
+        os.dup2(self.saved, 1)
+        os.close(self.saved)
+        return False
+
+
 METRIC = "particle-steps/s"
 WINDOW_STEPS = 500  # the pour configuration runs 500 steps
 # DRAM bytes (read + write) of one GJK-pass and one EPA-pass launch of this step, from the ncu capture
@@ -56,10 +75,15 @@ def parse():
     ap.add_argument("--pairs", type=int, default=1 << 22,
                     help="also time the narrow phase on this many independent random pairs (0: skip)")
     ap.add_argument("--pairs-only", action="store_true", help="only the independent-pair narrow-phase timing")
+    ap.add_argument("--pairs-lanes", default=None,
+                    help="lanes per pair for the pair timing, e.g. gjk1/epa16g (default: the sweep's best)")
     ap.add_argument("--batch-compare", action="store_true",
                     help="256 independent scenes (~2M particles): one batched graph step vs per-scene launches")
     ap.add_argument("--calibration", action="store_true",
                     help="differentiable calibration: 2,000 hulls, 5,000 steps, forward vs forward + adjoint")
+    ap.add_argument("--settling", action="store_true",
+                    help="config 1 (125 cubes, dt 1e-4, 2000 steps): the reference CPU path (oracle "
+                         "restatement, one core) and the device step")
     ap.add_argument("--calib-steps", type=int, default=5000)
     ap.add_argument("--calib-particles", type=int, default=2000)
     ap.add_argument("--contact-point", default="midpoint", choices=["reference", "midpoint"],
@@ -143,15 +167,16 @@ def cpu_path_rate(spec, max_seconds=20.0, max_steps=5):
     """Particle-steps/s of the reference path on the host (bounded sample: whole steps of the scene)."""
     s, kind = ref_kind(spec, None)
     n = spec.n_particles
-    s.step()  # warm-up (allocations, library load)
-    t0 = time.perf_counter()
-    steps = 0
-    while steps < max_steps:
-        s.step()
-        steps += 1
-        if time.perf_counter() - t0 > max_seconds:
-            break
-    dt = time.perf_counter() - t0
+    with host_prints_to_stderr():
+        s.step()  # warm-up (allocations, library load)
+        t0 = time.perf_counter()
+        steps = 0
+        while steps < max_steps:
+            s.step()
+            steps += 1
+            if time.perf_counter() - t0 > max_seconds:
+                break
+        dt = time.perf_counter() - t0
     cores = (os.cpu_count() or 1) if kind == "reference" else 1
     return {"value": n * steps / dt, "unit": METRIC, "cores": cores, "kind": kind,
             "sample": f"{steps} full steps of the {n}-particle pour after 1 warm-up step"}, s
@@ -207,13 +232,16 @@ def main():
         return reference_arm(args)
     torch.cuda.set_device(local)
     if args.pairs_only:
-        print(json.dumps({"narrow_pairs": pairs_rate(args.pairs, args.lanes)}), flush=True)
+        print(json.dumps({"narrow_pairs": pairs_rate(args.pairs, args.lanes, fixed=args.pairs_lanes)}), flush=True)
         return 0
     if args.batch_compare:
         print(json.dumps({"batch": batch_compare(args)}), flush=True)
         return 0
     if args.calibration:
         print(json.dumps({"calibration": calibration(args)}), flush=True)
+        return 0
+    if args.settling:
+        print(json.dumps({"settling": settling(args)}), flush=True)
         return 0
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
@@ -411,19 +439,31 @@ def pairs_cpu_rate(ps, n_pairs, sample=30_000, max_seconds=20.0):
     except Exception:
         kind, cores = "port", 1
         run = lambda d: oracle.contact(d, params, 2 * k, "f32")  # noqa: E731
-    done, t0 = 0, time.perf_counter()
-    for a in range(0, k, 10_000):
-        run({kk: v[a:a + 10_000] for kk, v in inp.items()})
-        done += min(10_000, k - a)
-        if time.perf_counter() - t0 > max_seconds:
-            break
-    dt = time.perf_counter() - t0
+    with host_prints_to_stderr():
+        done, t0 = 0, time.perf_counter()
+        for a in range(0, k, 10_000):
+            run({kk: v[a:a + 10_000] for kk, v in inp.items()})
+            done += min(10_000, k - a)
+            if time.perf_counter() - t0 > max_seconds:
+                break
+        dt = time.perf_counter() - t0
     return {"value": done / dt, "unit": "pairs/s", "cores": cores, "kind": kind,
             "sample": f"{done} of the {n_pairs} pairs (random, same seed; {dropped} pairs whose EPA overruns the "
                       f"reference's 50 faces or stops at its iteration cap left out), in chunks of 10,000"}
 
 
-def pairs_rate(n_pairs, lanes, reps=5, with_cpu=True):
+def parse_lanes(text):
+    """'gjk1/epa16gt' -> the lanes word (GJK lanes | EPA lanes << 8 | hulls read in place << 16 |
+    registers capped << 17)."""
+    import re
+    m = re.fullmatch(r"gjk(\d+)/epa(\d+)(g?)(t?)", text)
+    if not m:
+        raise SystemExit(f"bad lanes setting {text!r}; expected e.g. gjk1/epa16g")
+    return (int(m.group(1)) | (int(m.group(2)) << 8) | ((1 << 16) if m.group(3) else 0)
+            | ((1 << 17) if m.group(4) else 0))
+
+
+def pairs_rate(n_pairs, lanes, reps=5, with_cpu=True, fixed=None):
     """GJK/EPA pairs/s of the device-step narrow phase on independent random pairs (hulls of 8-64
     vertices, radius U[0.8,1.2], centre distance U[0.5,2.2] (rA+rB)/2; inputs ~10 GB, far above L2)."""
     import ctypes as C
@@ -435,9 +475,11 @@ def pairs_rate(n_pairs, lanes, reps=5, with_cpu=True):
     ps = PairScene(n_pairs, seed=1, lanes=lanes)
     stream = torch.cuda.current_stream()
     sweep = {}
-    cands = (8 | (8 << 8), 8 | (16 << 8), 4 | (16 << 8), 16 | (16 << 8), 4 | (16 << 8) | (1 << 16),
-             4 | (8 << 8) | (1 << 16), 8 | (16 << 8) | (1 << 16), 1 | (16 << 8), 1 | (16 << 8) | (1 << 16),
-             1 | (8 << 8) | (1 << 16))
+    cands = tuple(parse_lanes(t) for t in ("gjk8/epa8", "gjk8/epa16", "gjk4/epa16", "gjk4/epa16g", "gjk4/epa8g",
+                                           "gjk8/epa16g", "gjk1/epa16", "gjk1/epa16g", "gjk1/epa8g", "gjk1/epa16gt",
+                                           "gjk1/epa32gt", "gjk4/epa16gt"))
+    if fixed is not None:
+        cands = (parse_lanes(fixed),)
     for cand in cands:
         ps.lanes = cand
         ps.narrow()
@@ -519,6 +561,52 @@ def batch_compare(args):
             "particle_steps_per_s_sequential": n_total / (ms_seq * 1e-3),
             "batched_over_sequential": ms_seq / ms_batch, "identical_contact_sets": same,
             "status": batch.status(), "pairs_batched": int(len(bp))}
+
+
+def settling(args, steps=2000, cpu_seconds=20.0):
+    """Config 1: 125 randomly rotated unit cubes on a 5^3 lattice (spacing 1.5) settling onto a floor,
+    dt 1e-4, 2000 steps.  The reference CPU path (wall test + Linked_cell_hash + per-pair gather +
+    contact kernel FP32 + Verlet kernel FP64, as the oracle restates them) is timed on one host core
+    for the whole run or ~20 s, whichever ends first; the device step (graph replay) runs all 2000
+    steps."""
+    import torch
+    import stepper
+    from mwdiem_gb300 import scene
+    from mwdiem_gb300.sim import Simulator
+    spec = scene.settling_scene()
+    n = spec.n_particles
+    out = {"workload": "settling125: 125 unit cubes (density 1), 5x5x5 lattice at spacing 1.5, jitter 0.1, "
+                       "random orientations, floor 10x10, kn 1e5, damping ratio 0.3, mu 0.5, dt 1e-4",
+           "particles": n, "steps": steps}
+    # The reference's own contact kernel (built for the host) is not run here: once the cubes' contacts
+    # need more than 50 EPA faces it writes past its T[50]/V[50] arrays (gpu_fine_contact_detection.cu:
+    # 359-362, 519-539), which crashed the process on the Arm host.  The oracle's restatement computes
+    # the same results with bounded arrays, on one core.
+    s = stepper.RefStepper(spec, kind="port")
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps and time.perf_counter() - t0 < cpu_seconds:
+        s.step()
+        done += 1
+    dt = time.perf_counter() - t0
+    out["cpu_1core"] = {"value": n * done / dt, "unit": METRIC, "cores": 1, "kind": "port",
+                        "sample": f"the first {done} of the {steps} steps"}
+    sim = Simulator(spec)
+    per = 20  # steps per captured graph
+    sim.capture(steps_per_replay=per)
+    sim.replay(3)  # warm-up: the timed steps follow the first 61
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.replay(steps // per)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    out["gpu"] = {"value": n * steps / (ms * 1e-3), "unit": METRIC, "ms_per_step": ms / steps,
+                  "dtype": "f32 state, f64 centres", "graph_steps": per, "status": sim.status(),
+                  "sample": f"{steps} steps after 1 + {3 * per} warm-up steps"}
+    return out
 
 
 def calibration(args):
@@ -646,12 +734,13 @@ def reference_arm(args):
     spec = build_scene(SCENE["seed"])
     s, kind = ref_kind(spec, None)
     cores = (os.cpu_count() or 1) if kind == "reference" else 1
-    for _ in range(max(0, args.warmup)):
-        s.step()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        s.step()
-    dt = time.perf_counter() - t0
+    with host_prints_to_stderr():
+        for _ in range(max(0, args.warmup)):
+            s.step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s.step()
+        dt = time.perf_counter() - t0
     value = spec.n_particles * args.steps / dt
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,

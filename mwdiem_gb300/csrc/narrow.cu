@@ -95,12 +95,16 @@ __device__ __forceinline__ void support(const Group<LPP>& g, const float4* hA, i
     wk.queries += 1;
     float bA = -1e30f, bB = -1e30f;
     int iA = 0, iB = 0;
+    // unrolled so that several vertex loads are in flight (the scan order, and so the result, is
+    // unchanged)
+#pragma unroll 4
     for (int i = g.lane; i < nA; i += LPP) {
         float4 v = hA[i];
         float t = d.x * v.x + d.y * v.y + d.z * v.z;
         if (t > bA) { bA = t; iA = i; }
     }
     f3 nd = d * (-1.f);
+#pragma unroll 4
     for (int j = g.lane; j < nB; j += LPP) {
         float4 v = hB[j];
         float t = nd.x * v.x + nd.y * v.y + nd.z * v.z;
@@ -173,15 +177,41 @@ __device__ __forceinline__ void tet_test(f3 P1, f3 P2, f3 P3, f3 P4, int& coll, 
     else coll = 1;
 }
 
+// (double)v < 1e-6 && (double)v > -1e-6 for a float v, without FP64: a float compares with the
+// double 1e-6 as it compares with the smallest float not below it (0x358637be); NaN fails both
+__device__ __forceinline__ bool within_1e6(float v)
+{
+    const float F = __uint_as_float(0x358637beu);
+    return v < F && v > -F;
+}
+
 // CorrectFlat: both determinants inside a double +-1e-6 window (.cu:256-268)
 __device__ __forceinline__ bool is_flat(f3 S1, f3 S2, f3 S3, f3 S4)
 {
     float det1 = S1.x * (S2.y * S3.z - S3.y * S2.z) - S2.x * (S1.y * S3.z - S3.y * S1.z) + S3.x * (S1.y * S2.z - S2.y * S1.z);
-    if ((double)det1 < 0.000001 && (double)det1 > -0.000001) {
+    if (within_1e6(det1)) {
         float det2 = S1.x * (S2.y * S4.z - S4.y * S2.z) - S2.x * (S1.y * S4.z - S4.y * S1.z) + S4.x * (S1.y * S2.z - S2.y * S1.z);
-        if ((double)det2 < 0.000001 && (double)det2 > -0.000001) return true;
+        if (within_1e6(det2)) return true;
     }
     return false;
+}
+
+// The EPA's convergence test (.cu:439), (double)x * 1.00001 > (double)p && (double)x * 0.99999 <
+// (double)p, decided in FP32 unless p lies within 2^-22 |x| of one of the two bounds.  The float
+// products x * 1.00001f, x * 0.99999f are within 7.5e-8 |x| of the double ones and the shifted
+// bounds round by at most 6e-8 |x| more (1.4e-7 |x| < 2^-22 |x| in all), so outside that band the
+// float answer is the double one; inside it (and for |x| outside [1e-30, 1e37], NaN, or 0) the
+// double test runs.
+__device__ __forceinline__ bool epa_converged(float x, float p)
+{
+    const float ax = fabsf(x);
+    if (ax > 1e-30f && ax < 1e37f) {
+        const float hi = x * 1.00001f, lo = x * 0.99999f;
+        const float tol = ax * 2.384185791015625e-7f;
+        if (p < hi - tol && p > lo + tol) return true;
+        if (p > hi + tol || p < lo - tol) return false;
+    }
+    return (double)x * 1.00001 > (double)p && (double)x * 0.99999 < (double)p;
 }
 
 // AddTriangle (.cu:270-325), one face per calling lane
@@ -242,8 +272,9 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
     }
     g.sync();
     if (g.lane < 4) {
-        const int e[4][3] = {{0, 1, 2}, {1, 2, 3}, {2, 0, 3}, {0, 1, 3}};
-        add_face(m, e[g.lane][0], e[g.lane][1], e[g.lane][2], g.lane);
+        // faces (0,1,2), (1,2,3), (2,0,3), (0,1,3), packed as 4-bit vertex numbers (no local array)
+        const unsigned long long e = 0x310302321210ull >> (12 * g.lane);
+        add_face(m, (int)(e & 0xf), (int)((e >> 4) & 0xf), (int)((e >> 8) & 0xf), g.lane);
     }
     g.sync();
     wk.faces += 4;
@@ -275,7 +306,7 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
         int sa, sb;
         support<LPP>(g, hA, nA, hB, nB, n, s, sa, sb, wk);
         proj = dot(n, s);
-        if (xmin_old > proj || ((double)xmin_old * 1.00001 > (double)proj && (double)xmin_old * 0.99999 < (double)proj)) break;
+        if (xmin_old > proj || epa_converged(xmin_old, proj)) break;
         if (counter > 49) { r.status |= MWD_ST_EPA_NOCONV; break; }
         counter = counter + 1;
         if (nv >= VCAP) { r.status |= MWD_ST_EPA_OVERFLOW; break; }
@@ -948,8 +979,10 @@ __global__ void hist_flip_kernel(NarrowArgs a)
     if (threadIdx.x == 0 && blockIdx.x == 0) *a.hist_parity ^= 1;
 }
 
-template <int LPP>
-__global__ void __launch_bounds__(NARROW_THREADS) epa_pass_kernel(NarrowArgs a)
+// registers capped for 5 blocks of 128 threads per SM, or with TIGHT for 7 (a few spills, more pairs
+// in flight)
+template <int LPP, int TIGHT>
+__global__ void __launch_bounds__(NARROW_THREADS, TIGHT ? 7 : 5) epa_pass_kernel(NarrowArgs a)
 {
     pdl_wait();
     pdl_launch_dependents();
@@ -1026,7 +1059,7 @@ __global__ void __launch_bounds__(NARROW_THREADS) epa_pass_kernel(NarrowArgs a)
     }
 }
 
-template <int LPP, int ELPP>
+template <int LPP, int ELPP, int TIGHT>
 int launch_two_pass_lpp(const NarrowArgs& a, cudaStream_t s)
 {
     constexpr int GPB = NARROW_THREADS / ELPP;
@@ -1042,19 +1075,20 @@ int launch_two_pass_lpp(const NarrowArgs& a, cudaStream_t s)
     }
     const size_t shm = (size_t)GPB * sizeof(EpaMem) + (a.epa_global ? 0 : (size_t)GPB * 2 * a.hull_cap * sizeof(float4));
     if (!attr) {
-        MWD_CUDA(cudaFuncSetAttribute(epa_pass_kernel<ELPP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        MWD_CUDA(cudaFuncSetAttribute(epa_pass_kernel<ELPP, TIGHT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      200 * 1024));
         attr = true;
     }
     if (shm != epa_shm_cached || !epa_per_sm) {
         int v = 0;
-        MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, epa_pass_kernel<ELPP>, NARROW_THREADS, shm));
+        MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, epa_pass_kernel<ELPP, TIGHT>, NARROW_THREADS, shm));
         epa_per_sm = v < 1 ? 1 : v;
         epa_shm_cached = shm;
     }
     if (!a.epa_zeroed) MWD_CUDA(cudaMemsetAsync(a.epa_count, 0, sizeof(int32_t), s));
     if (a.hist_keys) MWD_CUDA(launch_pdl(hist_clear_kernel, (unsigned)(num_sms() * 4), 256, 0, s, a));
     MWD_CUDA(launch_pdl(gjk_pass_kernel<LPP>, (unsigned)(num_sms() * gjk_per_sm), NARROW_THREADS, 0, s, a));
-    MWD_CUDA(launch_pdl(epa_pass_kernel<ELPP>, (unsigned)(num_sms() * epa_per_sm), NARROW_THREADS, shm, s, a));
+    MWD_CUDA(launch_pdl(epa_pass_kernel<ELPP, TIGHT>, (unsigned)(num_sms() * epa_per_sm), NARROW_THREADS, shm, s, a));
     if (a.hist_keys) MWD_CUDA(launch_pdl(hist_flip_kernel, 1, 32, 0, s, a));
     return MWD_OK;
 }
@@ -1133,13 +1167,16 @@ int launch_narrow(const NarrowArgs& a, int mode, int lanes, int64_t n_hint, cuda
     return MWD_ERR_INVALID;
 }
 
-// lanes = GJK-pass lanes per pair | EPA-pass lanes per pair << 8 (EPA lanes 0: same as GJK)
+// lanes = GJK-pass lanes per pair | EPA-pass lanes per pair << 8 (EPA lanes 0: same as GJK);
+// hulls in place and the register cap of the EPA pass come in NarrowArgs (epa_global, epa_tight)
 int launch_narrow_two_pass(const NarrowArgs& a, int lanes, cudaStream_t s)
 {
     const int gl = lanes & 0xff;
     int el = (lanes >> 8) & 0xff;
     if (!el) el = gl;
-#define MWD_TP(G, E) if (gl == G && el == E) return launch_two_pass_lpp<G, E>(a, s)
+#define MWD_TP(G, E)                                                                         \
+    if (gl == G && el == E)                                                                  \
+        return a.epa_tight ? launch_two_pass_lpp<G, E, 1>(a, s) : launch_two_pass_lpp<G, E, 0>(a, s)
     MWD_TP(1, 4); MWD_TP(1, 8); MWD_TP(1, 16); MWD_TP(1, 32);
     MWD_TP(4, 4); MWD_TP(4, 8); MWD_TP(4, 16); MWD_TP(4, 32);
     MWD_TP(8, 8); MWD_TP(8, 16); MWD_TP(8, 32); MWD_TP(8, 4);

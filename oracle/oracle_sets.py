@@ -53,11 +53,23 @@ def pairs_set(kn=1e5, zeta=0.3, mu=0.5, dt=5e-5, V=64):
                 num_particles_wall=0, timestep=dt)
 
 
+def settling_sets():
+    """Contact and integrator parameter sets of the 125-cube settling scene, as the reference path
+    (oracle/stepper.py) derives them from the scene."""
+    import stepper
+    from mwdiem_gb300 import scene
+    s = stepper.RefStepper(scene.settling_scene(), kind="port")
+    return dict(s.params), s.verlet_params()
+
+
 def render_all():
     c, v = pour_sets()
     register_contact(c)
     register_verlet(v)
     register_contact(pairs_set())
+    c, v = settling_sets()
+    register_contact(c)
+    register_verlet(v)
     out = []
     for p in CONTACT_SETS:
         out.append(build_ref.ensure_built("contact", p, "f32"))
