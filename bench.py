@@ -232,7 +232,8 @@ def main():
         return reference_arm(args)
     torch.cuda.set_device(local)
     if args.pairs_only:
-        print(json.dumps({"narrow_pairs": pairs_rate(args.pairs, args.lanes, fixed=args.pairs_lanes)}), flush=True)
+        print(json.dumps({"narrow_pairs": pairs_rate(args.pairs, args.lanes, with_cpu=not args.no_cpu_baseline,
+                                                     fixed=args.pairs_lanes)}), flush=True)
         return 0
     if args.batch_compare:
         print(json.dumps({"batch": batch_compare(args)}), flush=True)

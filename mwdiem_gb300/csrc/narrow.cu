@@ -379,6 +379,9 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
     }
     g.sync();
     r.depth = xmin_new;
+    // the contact point and everything after it (the force) are needed by one lane only: the others
+    // skip them, which keeps their FP64 operations (below and in contact_force) off the FP64 pipe
+    if (g.lane != 0) return;
     uint32_t t = m.ft[indmin];
     int a = ft_v(t, 0), b = ft_v(t, 1), c = ft_v(t, 2);
     f3 n = xyz(m.fn[indmin]);
@@ -670,10 +673,12 @@ __device__ void process_pair(const NarrowArgs& a, int64_t P, const Group<LPP>& g
                     support<LPP>(g, hA, p.nA, hB, p.nB, d4, S4, a4, b4, wk);
                 }
                 epa<LPP>(g, em, hA, p.nA, hB, p.nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er, wk);
-                float imA, imB;
-                pair_inv_mass<MODE>(a, p, M, imA, imB);
-                contact_force(p.cA, p.cB, er.depth, er.n, er.cpA, er.cpB, M, p.vA, p.vB, p.wA, p.wB, p.dt, p.qA,
-                              p.dtn, p.IsA, p.IsB, imA, imB, fo);
+                if (leader) {
+                    float imA, imB;
+                    pair_inv_mass<MODE>(a, p, M, imA, imB);
+                    contact_force(p.cA, p.cB, er.depth, er.n, er.cpA, er.cpB, M, p.vA, p.vB, p.wA, p.wB, p.dt,
+                                  p.qA, p.dtn, p.IsA, p.IsB, imA, imB, fo);
+                }
                 st |= er.status;
                 resolved = true;
                 break;
@@ -1026,12 +1031,12 @@ __global__ void __launch_bounds__(NARROW_THREADS, TIGHT ? 7 : 5) epa_pass_kernel
         }
         EpaResult er;
         epa<LPP>(g, *em, hA, p.nA, hB, p.nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er, wk);
-        ForceResult fo;
-        float imA, imB;
-        pair_inv_mass<1>(a, p, M, imA, imB);
-        contact_force(p.cA, p.cB, er.depth, er.n, er.cpA, er.cpB, M, p.vA, p.vB, p.wA, p.wB, p.dt, p.qA, p.dtn, p.IsA,
-                      p.IsB, imA, imB, fo);
         if (g.lane == 0) {
+            ForceResult fo;
+            float imA, imB;
+            pair_inv_mass<1>(a, p, M, imA, imB);
+            contact_force(p.cA, p.cB, er.depth, er.n, er.cpA, er.cpB, M, p.vA, p.vB, p.wA, p.wB, p.dt, p.qA, p.dtn,
+                          p.IsA, p.IsB, imA, imB, fo);
             set_status(a.status, er.status);
             if (a.hist_keys) hist_put(a, p.idA, p.idB, fo.dt);
             if (a.det_out) {
