@@ -67,7 +67,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--lanes", type=int, default=8)
+    ap.add_argument("--lanes", type=lanes_arg, default=8,
+                    help="lanes per pair: an integer, or a setting such as gjk8/epa32g (with --no-tune)")
     ap.add_argument("--no-tune", action="store_true", help="use --lanes instead of the autotuner's choice")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -453,15 +454,17 @@ def pairs_cpu_rate(ps, n_pairs, sample=30_000, max_seconds=20.0):
                       f"reference's 50 faces or stops at its iteration cap left out), in chunks of 10,000"}
 
 
+def lanes_arg(text):
+    return parse_lanes(text) if "/" in str(text) else int(text)
+
+
 def parse_lanes(text):
-    """'gjk1/epa16gt' -> the lanes word (GJK lanes | EPA lanes << 8 | hulls read in place << 16 |
-    registers capped << 17)."""
+    """'gjk1/epa16g' -> the lanes word (GJK lanes | EPA lanes << 8 | hulls read in place << 16)."""
     import re
-    m = re.fullmatch(r"gjk(\d+)/epa(\d+)(g?)(t?)", text)
+    m = re.fullmatch(r"gjk(\d+)/epa(\d+)(g?)", text)
     if not m:
         raise SystemExit(f"bad lanes setting {text!r}; expected e.g. gjk1/epa16g")
-    return (int(m.group(1)) | (int(m.group(2)) << 8) | ((1 << 16) if m.group(3) else 0)
-            | ((1 << 17) if m.group(4) else 0))
+    return int(m.group(1)) | (int(m.group(2)) << 8) | ((1 << 16) if m.group(3) else 0)
 
 
 def pairs_rate(n_pairs, lanes, reps=5, with_cpu=True, fixed=None):
@@ -477,8 +480,7 @@ def pairs_rate(n_pairs, lanes, reps=5, with_cpu=True, fixed=None):
     stream = torch.cuda.current_stream()
     sweep = {}
     cands = tuple(parse_lanes(t) for t in ("gjk8/epa8", "gjk8/epa16", "gjk4/epa16", "gjk4/epa16g", "gjk4/epa8g",
-                                           "gjk8/epa16g", "gjk1/epa16", "gjk1/epa16g", "gjk1/epa8g", "gjk1/epa16gt",
-                                           "gjk1/epa32gt", "gjk4/epa16gt"))
+                                           "gjk8/epa16g", "gjk1/epa16", "gjk1/epa16g", "gjk1/epa8g", "gjk1/epa32g"))
     if fixed is not None:
         cands = (parse_lanes(fixed),)
     for cand in cands:

@@ -332,8 +332,7 @@ int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_s
  * lanes: lanes per pair of the GJK pass (1 with the two-pass kernel, 4, 8, 16, 32), plus, in bits
  * 8-15, those of the EPA pass of the two-pass kernel (0: the same); bit 16 set: the EPA pass reads
  * the hulls in place from the vertex table instead of staging them in shared memory (less shared
- * memory, more resident pairs); bit 17 set: the EPA pass kernel built with registers capped for
- * 7 blocks per SM (a few spills, more resident pairs). */
+ * memory, more resident pairs). */
 int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work* work,
                      int32_t lanes, mwd_stream_t stream);
 

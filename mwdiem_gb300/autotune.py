@@ -1,8 +1,7 @@
 """Autotuner for the device-resident step.
 
-Chooses the lanes per pair of the narrow phase's GJK pass (1, 4, 8 or 16) and EPA pass (8, 16 or 32),
-whether the EPA pass stages the two hulls in shared memory or reads them in place, and whether its
-registers are capped for occupancy, by timing graph-captured steps of the actual scene and keeping
+Chooses the lanes per pair of the narrow phase's GJK pass (1, 4, 8 or 16) and EPA pass (8, 16 or 32)
+and whether the EPA pass stages the two hulls in shared memory or reads them in place, by timing graph-captured steps of the actual scene and keeping
 the fastest.  The
 cell size is not a tuning knob: it decides the reference's candidate set (an 8-cell forward stencil
 misses some neighbour pairs, and which ones depends on the cell size), so it stays what the scene
@@ -32,16 +31,13 @@ def time_steps(sim, steps=5, reps=3):
 
 
 # lanes word: GJK-pass lanes | EPA-pass lanes << 8 | EPA hulls read in place (no staging) << 16
-#             | EPA pass with registers capped for 7 blocks per SM << 17
 EPA_IN_PLACE = 1 << 16
-EPA_TIGHT = 1 << 17
-DEFAULT_CANDIDATES = tuple(g | (e << 8) | f for g in (1, 4, 8, 16) for e in (8, 16, 32) for f in (0, EPA_IN_PLACE)) + \
-    tuple(g | (e << 8) | EPA_IN_PLACE | EPA_TIGHT for g in (1, 4, 8, 16) for e in (16, 32))
+DEFAULT_CANDIDATES = tuple(g | (e << 8) | f for g in (1, 4, 8, 16) for e in (8, 16, 32) for f in (0, EPA_IN_PLACE))
 
 
 def describe(lanes):
     s = f"gjk{lanes & 0xff}/epa{((lanes >> 8) & 0xff) or (lanes & 0xff)}"
-    return s + ("g" if lanes & EPA_IN_PLACE else "") + ("t" if lanes & EPA_TIGHT else "")
+    return s + ("g" if lanes & EPA_IN_PLACE else "")
 
 
 def tune_lanes(sim, candidates=DEFAULT_CANDIDATES, steps=5):

@@ -448,7 +448,6 @@ static int narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_wo
     const int elp = (lanes >> 8) & 0xff;
     NarrowArgs a = {};
     a.epa_global = (lanes >> 16) & 1;
-    a.epa_tight = (lanes >> 17) & 1;
     a.st = *st;
     a.scenes = scenes_dev;
     a.pairs = work->pairs;

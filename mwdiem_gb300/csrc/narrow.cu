@@ -831,6 +831,85 @@ __device__ int gjk_decide(const Group<LPP>& g, const float4* hA, int nA, const f
     return -1;
 }
 
+// GJK on pair P by the group; lane 0 records the outcome (status, contact flag, and for a pair in
+// contact its simplex in the EPA list, whose slot it also appends to *list when list is given)
+template <int LPP>
+__device__ __forceinline__ void gjk_pair(const NarrowArgs& a, const Group<LPP>& g, int64_t P, int* list, int* list_n)
+{
+    const double4* pos = reinterpret_cast<const double4*>(a.st.pos);
+    const int2* pairs = reinterpret_cast<const int2*>(a.pairs);
+    const float4* wv = reinterpret_cast<const float4*>(a.st.world_verts);
+    SimplexRec* recs = reinterpret_cast<SimplexRec*>(a.epa_rec);
+    const int2 pr = pairs[P];
+    const double4 pa = pos[pr.x], pb = pos[pr.y];
+    const f3 cA = mk3((float)pa.x, (float)pa.y, (float)pa.z);
+    const f3 cB = mk3((float)pb.x, (float)pb.y, (float)pb.z);
+    const int oa = a.st.vert_off[pr.x], ob = a.st.vert_off[pr.y];
+    const int nA = a.st.vert_off[pr.x + 1] - oa, nB = a.st.vert_off[pr.y + 1] - ob;
+    Work3 wk = {0u, 0u, 0u};
+    SimplexRec rec;
+    int out = 0;
+    const bool ok = nA <= a.hull_cap && nB <= a.hull_cap;
+    if (ok) out = gjk_decide<LPP>(g, wv + oa, nA, wv + ob, nB, cA, cB, rec, wk);
+    if (g.lane == 0) {
+        if (!ok) {
+            set_status(a.status, MWD_ST_BAD_SHAPE);
+            if (a.collision) a.collision[P] = -1;
+        } else if (out == 1) {
+            const int slot = atomicAdd(a.epa_count, 1);
+            if (slot < a.epa_cap) {
+                rec.P = P;
+                recs[slot] = rec;
+                if (list) list[atomicAdd(list_n, 1)] = slot;
+            } else {
+                set_status(a.status, MWD_ST_PAIR_OVERFLOW);
+            }
+            if (a.collision) a.collision[P] = 1;
+        } else {
+            // undecided pairs add zero force in the reference (.cu:1304-1319): nothing to add
+            if (out == -1) set_status(a.status, MWD_ST_GJK_NOCONV);
+            if (a.collision) a.collision[P] = out;
+        }
+        if (a.work_counters) {
+            atomicAdd(a.work_counters + 0, (unsigned long long)wk.dots);
+            atomicAdd(a.work_counters + 2, (unsigned long long)wk.queries);
+        }
+    }
+    g.sync();
+}
+
+// GJK on the candidates [base, base + chunk), clipped to hi, by one group (chunk = gjk_chunk(a, LPP)).
+// pre_culled: the broad phase already dropped the pairs whose spheres are apart, so each chunk is one
+// pair and it runs GJK; otherwise the chunk's LPP candidates are sphere-tested at once (one per lane)
+// and the survivors run GJK one after another.
+__device__ __forceinline__ int gjk_chunk(const NarrowArgs& a, int lpp) { return a.pre_culled ? 1 : lpp; }
+
+template <int LPP>
+__device__ __forceinline__ void gjk_candidates(const NarrowArgs& a, const Group<LPP>& g, int64_t base, int64_t hi,
+                                               int* list, int* list_n)
+{
+    unsigned msk;
+    if (a.pre_culled) {
+        msk = 1u;
+    } else {
+        const double4* pos = reinterpret_cast<const double4*>(a.st.pos);
+        const int2* pairs = reinterpret_cast<const int2*>(a.pairs);
+        const int64_t Pl = base + g.lane;
+        bool live = false;
+        if (Pl < hi) {
+            const int2 pr = pairs[Pl];
+            live = !spheres_apart(pos[pr.x], pos[pr.y]);
+            if (!live && a.collision) a.collision[Pl] = 0;
+        }
+        msk = g.ballot(live);
+    }
+    while (msk) {
+        const int l = __ffs(msk) - 1;
+        msk &= msk - 1;
+        gjk_pair<LPP>(a, g, base + l, list, list_n);
+    }
+}
+
 template <int LPP>
 __global__ void __launch_bounds__(NARROW_THREADS, 6) gjk_pass_kernel(NarrowArgs a)
 {
@@ -843,70 +922,10 @@ __global__ void __launch_bounds__(NARROW_THREADS, 6) gjk_pass_kernel(NarrowArgs 
     g.mask = LPP == 32 ? 0xffffffffu : (((1u << LPP) - 1u) << ((threadIdx.x & 31) / LPP * LPP));
     const int64_t m = *a.n_pairs_dev;
     const int64_t n = m < a.pair_cap ? m : a.pair_cap;
-    const double4* pos = reinterpret_cast<const double4*>(a.st.pos);
-    const int2* pairs = reinterpret_cast<const int2*>(a.pairs);
-    const float4* wv = reinterpret_cast<const float4*>(a.st.world_verts);
-    SimplexRec* recs = reinterpret_cast<SimplexRec*>(a.epa_rec);
-    // pre_culled: the broad phase already dropped the pairs whose spheres are apart, so every listed
-    // pair needs GJK and each group takes one pair at a time; otherwise LPP candidates are
-    // sphere-tested at once (one per lane) and the survivors run GJK
-    const int chunk = a.pre_culled ? 1 : LPP;
+    const int chunk = gjk_chunk(a, LPP);
     const int64_t stride = (int64_t)gridDim.x * GPB * chunk;
-    for (int64_t base = ((int64_t)blockIdx.x * GPB + grp) * chunk; base < n; base += stride) {
-        unsigned msk;
-        if (a.pre_culled) {
-            msk = 1u;
-        } else {
-            const int64_t Pl = base + g.lane;
-            bool live = false;
-            if (Pl < n) {
-                const int2 pr = pairs[Pl];
-                live = !spheres_apart(pos[pr.x], pos[pr.y]);
-                if (!live && a.collision) a.collision[Pl] = 0;
-            }
-            msk = g.ballot(live);
-        }
-        while (msk) {
-            const int l = __ffs(msk) - 1;
-            msk &= msk - 1;
-            const int64_t P = base + l;
-            const int2 pr = pairs[P];
-            const double4 pa = pos[pr.x], pb = pos[pr.y];
-            const f3 cA = mk3((float)pa.x, (float)pa.y, (float)pa.z);
-            const f3 cB = mk3((float)pb.x, (float)pb.y, (float)pb.z);
-            const int oa = a.st.vert_off[pr.x], ob = a.st.vert_off[pr.y];
-            const int nA = a.st.vert_off[pr.x + 1] - oa, nB = a.st.vert_off[pr.y + 1] - ob;
-            Work3 wk = {0u, 0u, 0u};
-            SimplexRec rec;
-            int out = 0;
-            const bool ok = nA <= a.hull_cap && nB <= a.hull_cap;
-            if (ok) out = gjk_decide<LPP>(g, wv + oa, nA, wv + ob, nB, cA, cB, rec, wk);
-            if (g.lane == 0) {
-                if (!ok) {
-                    set_status(a.status, MWD_ST_BAD_SHAPE);
-                    if (a.collision) a.collision[P] = -1;
-                } else if (out == 1) {
-                    const int slot = atomicAdd(a.epa_count, 1);
-                    if (slot < a.epa_cap) {
-                        rec.P = P;
-                        recs[slot] = rec;
-                    } else {
-                        set_status(a.status, MWD_ST_PAIR_OVERFLOW);
-                    }
-                    if (a.collision) a.collision[P] = 1;
-                } else {
-                    // undecided pairs add zero force in the reference (.cu:1304-1319): nothing to add
-                    if (out == -1) set_status(a.status, MWD_ST_GJK_NOCONV);
-                    if (a.collision) a.collision[P] = out;
-                }
-                if (a.work_counters) {
-                    atomicAdd(a.work_counters + 0, (unsigned long long)wk.dots);
-                    atomicAdd(a.work_counters + 2, (unsigned long long)wk.queries);
-                }
-            }
-            g.sync();
-        }
-    }
+    for (int64_t base = ((int64_t)blockIdx.x * GPB + grp) * chunk; base < n; base += stride)
+        gjk_candidates<LPP>(a, g, base, n, nullptr, nullptr);
 }
 
 // ------------------------------------------------------------------ persistent tangential history
@@ -984,10 +1003,76 @@ __global__ void hist_flip_kernel(NarrowArgs a)
     if (threadIdx.x == 0 && blockIdx.x == 0) *a.hist_parity ^= 1;
 }
 
-// registers capped for 5 blocks of 128 threads per SM, or with TIGHT for 7 (a few spills, more pairs
-// in flight)
-template <int LPP, int TIGHT>
-__global__ void __launch_bounds__(NARROW_THREADS, TIGHT ? 7 : 5) epa_pass_kernel(NarrowArgs a)
+// CorrectFlat, EPA, force and the outputs for EPA record i, by one group (em: its polytope; hull:
+// its staging area when the hulls are staged)
+template <int LPP>
+__device__ __forceinline__ void epa_record(const NarrowArgs& a, const Group<LPP>& g, EpaMem* em, float4* hull,
+                                           int64_t i)
+{
+    const float4* wv = reinterpret_cast<const float4*>(a.st.world_verts);
+    const SimplexRec* recs = reinterpret_cast<const SimplexRec*>(a.epa_rec);
+    const SimplexRec rec = recs[i];
+    const int64_t P = rec.P;
+    PairView p;
+    // the hulls staged in shared memory, or read in place from the (L1-cached) vertex table
+    const float4* hA = hull;
+    const float4* hB = hull + a.hull_cap;
+    load_pair<1>(a, P, p, hull, hull + a.hull_cap, g.lane, LPP, !a.epa_global);
+    if (a.epa_global) {
+        hA = wv + a.st.vert_off[p.idA];
+        hB = wv + a.st.vert_off[p.idB];
+    }
+    if (a.hist_keys) {
+        p.dt = hist_get(a, p.idA, p.idB);
+        p.dtn = sqrtf(p.dt.x * p.dt.x + p.dt.y * p.dt.y + p.dt.z * p.dt.z);
+    }
+    g.sync();
+    const mwd_material& M = a.scenes[a.st.info[p.idA] >> 1].mat[p.wall];
+    Work3 wk = {0u, 0u, 0u};
+    f3 S1 = xyz(rec.S[0]), S2 = xyz(rec.S[1]), S3 = xyz(rec.S[2]), S4 = xyz(rec.S[3]);
+    int a1 = rec.ia & 0xff, a2 = (rec.ia >> 8) & 0xff, a3 = (rec.ia >> 16) & 0xff, a4 = rec.ia >> 24;
+    int b1 = rec.ib & 0xff, b2 = (rec.ib >> 8) & 0xff, b3 = (rec.ib >> 16) & 0xff, b4 = rec.ib >> 24;
+    if (is_flat(S1, S2, S3, S4)) {
+        f3 d4 = cross(S1, S2);
+        support<LPP>(g, hA, p.nA, hB, p.nB, d4, S4, a4, b4, wk);
+    }
+    EpaResult er;
+    epa<LPP>(g, *em, hA, p.nA, hB, p.nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er, wk);
+    if (g.lane == 0) {
+        ForceResult fo;
+        float imA, imB;
+        pair_inv_mass<1>(a, p, M, imA, imB);
+        contact_force(p.cA, p.cB, er.depth, er.n, er.cpA, er.cpB, M, p.vA, p.vB, p.wA, p.wB, p.dt, p.qA, p.dtn,
+                      p.IsA, p.IsB, imA, imB, fo);
+        set_status(a.status, er.status);
+        if (a.hist_keys) hist_put(a, p.idA, p.idB, fo.dt);
+        if (a.det_out) {
+            float4* o = a.det_out + 3 * i;
+            o[0] = f4(fo.F, 0.f);
+            o[1] = f4(fo.TA, 0.f);
+            o[2] = f4(fo.TB, 0.f);
+        } else {
+            accumulate<1>(a, p, fo);
+        }
+        if (a.face_ids) {
+            int* fid = a.face_ids + 6 * P;
+            for (int k = 0; k < 3; ++k) {
+                fid[k] = er.fa[k];
+                fid[3 + k] = er.fb[k];
+            }
+        }
+        if (a.work_counters) {
+            atomicAdd(a.work_counters + 0, (unsigned long long)wk.dots);
+            atomicAdd(a.work_counters + 1, (unsigned long long)wk.faces);
+            atomicAdd(a.work_counters + 2, (unsigned long long)wk.queries);
+        }
+    }
+    g.sync();
+}
+
+// registers capped for 5 blocks of 128 threads per SM
+template <int LPP>
+__global__ void __launch_bounds__(NARROW_THREADS, 5) epa_pass_kernel(NarrowArgs a)
 {
     pdl_wait();
     pdl_launch_dependents();
@@ -999,72 +1084,13 @@ __global__ void __launch_bounds__(NARROW_THREADS, TIGHT ? 7 : 5) epa_pass_kernel
     g.mask = LPP == 32 ? 0xffffffffu : (((1u << LPP) - 1u) << ((threadIdx.x & 31) / LPP * LPP));
     EpaMem* em = reinterpret_cast<EpaMem*>(smem) + grp;
     float4* hull = reinterpret_cast<float4*>(reinterpret_cast<EpaMem*>(smem) + GPB) + (size_t)grp * 2 * a.hull_cap;
-    const float4* wv = reinterpret_cast<const float4*>(a.st.world_verts);
     const int cnt = *a.epa_count;
     const int64_t m = cnt < a.epa_cap ? cnt : a.epa_cap;
-    const SimplexRec* recs = reinterpret_cast<const SimplexRec*>(a.epa_rec);
-    for (int64_t i = (int64_t)blockIdx.x * GPB + grp; i < m; i += (int64_t)gridDim.x * GPB) {
-        const SimplexRec rec = recs[i];
-        const int64_t P = rec.P;
-        PairView p;
-        // the hulls staged in shared memory, or read in place from the (L1-cached) vertex table
-        const float4* hA = hull;
-        const float4* hB = hull + a.hull_cap;
-        load_pair<1>(a, P, p, hull, hull + a.hull_cap, g.lane, LPP, !a.epa_global);
-        if (a.epa_global) {
-            hA = wv + a.st.vert_off[p.idA];
-            hB = wv + a.st.vert_off[p.idB];
-        }
-        if (a.hist_keys) {
-            p.dt = hist_get(a, p.idA, p.idB);
-            p.dtn = sqrtf(p.dt.x * p.dt.x + p.dt.y * p.dt.y + p.dt.z * p.dt.z);
-        }
-        g.sync();
-        const mwd_material& M = a.scenes[a.st.info[p.idA] >> 1].mat[p.wall];
-        Work3 wk = {0u, 0u, 0u};
-        f3 S1 = xyz(rec.S[0]), S2 = xyz(rec.S[1]), S3 = xyz(rec.S[2]), S4 = xyz(rec.S[3]);
-        int a1 = rec.ia & 0xff, a2 = (rec.ia >> 8) & 0xff, a3 = (rec.ia >> 16) & 0xff, a4 = rec.ia >> 24;
-        int b1 = rec.ib & 0xff, b2 = (rec.ib >> 8) & 0xff, b3 = (rec.ib >> 16) & 0xff, b4 = rec.ib >> 24;
-        if (is_flat(S1, S2, S3, S4)) {
-            f3 d4 = cross(S1, S2);
-            support<LPP>(g, hA, p.nA, hB, p.nB, d4, S4, a4, b4, wk);
-        }
-        EpaResult er;
-        epa<LPP>(g, *em, hA, p.nA, hB, p.nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er, wk);
-        if (g.lane == 0) {
-            ForceResult fo;
-            float imA, imB;
-            pair_inv_mass<1>(a, p, M, imA, imB);
-            contact_force(p.cA, p.cB, er.depth, er.n, er.cpA, er.cpB, M, p.vA, p.vB, p.wA, p.wB, p.dt, p.qA, p.dtn,
-                          p.IsA, p.IsB, imA, imB, fo);
-            set_status(a.status, er.status);
-            if (a.hist_keys) hist_put(a, p.idA, p.idB, fo.dt);
-            if (a.det_out) {
-                float4* o = a.det_out + 3 * i;
-                o[0] = f4(fo.F, 0.f);
-                o[1] = f4(fo.TA, 0.f);
-                o[2] = f4(fo.TB, 0.f);
-            } else {
-                accumulate<1>(a, p, fo);
-            }
-            if (a.face_ids) {
-                int* fid = a.face_ids + 6 * P;
-                for (int k = 0; k < 3; ++k) {
-                    fid[k] = er.fa[k];
-                    fid[3 + k] = er.fb[k];
-                }
-            }
-            if (a.work_counters) {
-                atomicAdd(a.work_counters + 0, (unsigned long long)wk.dots);
-                atomicAdd(a.work_counters + 1, (unsigned long long)wk.faces);
-                atomicAdd(a.work_counters + 2, (unsigned long long)wk.queries);
-            }
-        }
-        g.sync();
-    }
+    for (int64_t i = (int64_t)blockIdx.x * GPB + grp; i < m; i += (int64_t)gridDim.x * GPB)
+        epa_record<LPP>(a, g, em, hull, i);
 }
 
-template <int LPP, int ELPP, int TIGHT>
+template <int LPP, int ELPP>
 int launch_two_pass_lpp(const NarrowArgs& a, cudaStream_t s)
 {
     constexpr int GPB = NARROW_THREADS / ELPP;
@@ -1080,20 +1106,20 @@ int launch_two_pass_lpp(const NarrowArgs& a, cudaStream_t s)
     }
     const size_t shm = (size_t)GPB * sizeof(EpaMem) + (a.epa_global ? 0 : (size_t)GPB * 2 * a.hull_cap * sizeof(float4));
     if (!attr) {
-        MWD_CUDA(cudaFuncSetAttribute(epa_pass_kernel<ELPP, TIGHT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        MWD_CUDA(cudaFuncSetAttribute(epa_pass_kernel<ELPP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       200 * 1024));
         attr = true;
     }
     if (shm != epa_shm_cached || !epa_per_sm) {
         int v = 0;
-        MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, epa_pass_kernel<ELPP, TIGHT>, NARROW_THREADS, shm));
+        MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, epa_pass_kernel<ELPP>, NARROW_THREADS, shm));
         epa_per_sm = v < 1 ? 1 : v;
         epa_shm_cached = shm;
     }
     if (!a.epa_zeroed) MWD_CUDA(cudaMemsetAsync(a.epa_count, 0, sizeof(int32_t), s));
     if (a.hist_keys) MWD_CUDA(launch_pdl(hist_clear_kernel, (unsigned)(num_sms() * 4), 256, 0, s, a));
     MWD_CUDA(launch_pdl(gjk_pass_kernel<LPP>, (unsigned)(num_sms() * gjk_per_sm), NARROW_THREADS, 0, s, a));
-    MWD_CUDA(launch_pdl(epa_pass_kernel<ELPP, TIGHT>, (unsigned)(num_sms() * epa_per_sm), NARROW_THREADS, shm, s, a));
+    MWD_CUDA(launch_pdl(epa_pass_kernel<ELPP>, (unsigned)(num_sms() * epa_per_sm), NARROW_THREADS, shm, s, a));
     if (a.hist_keys) MWD_CUDA(launch_pdl(hist_flip_kernel, 1, 32, 0, s, a));
     return MWD_OK;
 }
@@ -1172,16 +1198,14 @@ int launch_narrow(const NarrowArgs& a, int mode, int lanes, int64_t n_hint, cuda
     return MWD_ERR_INVALID;
 }
 
-// lanes = GJK-pass lanes per pair | EPA-pass lanes per pair << 8 (EPA lanes 0: same as GJK);
-// hulls in place and the register cap of the EPA pass come in NarrowArgs (epa_global, epa_tight)
+// lanes = GJK-pass lanes per pair | EPA-pass lanes per pair << 8 (EPA lanes 0: same as GJK); whether
+// the EPA pass reads the hulls in place comes in NarrowArgs (epa_global)
 int launch_narrow_two_pass(const NarrowArgs& a, int lanes, cudaStream_t s)
 {
     const int gl = lanes & 0xff;
     int el = (lanes >> 8) & 0xff;
     if (!el) el = gl;
-#define MWD_TP(G, E)                                                                         \
-    if (gl == G && el == E)                                                                  \
-        return a.epa_tight ? launch_two_pass_lpp<G, E, 1>(a, s) : launch_two_pass_lpp<G, E, 0>(a, s)
+#define MWD_TP(G, E) if (gl == G && el == E) return launch_two_pass_lpp<G, E>(a, s)
     MWD_TP(1, 4); MWD_TP(1, 8); MWD_TP(1, 16); MWD_TP(1, 32);
     MWD_TP(4, 4); MWD_TP(4, 8); MWD_TP(4, 16); MWD_TP(4, 32);
     MWD_TP(8, 8); MWD_TP(8, 16); MWD_TP(8, 32); MWD_TP(8, 4);

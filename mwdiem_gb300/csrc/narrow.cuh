@@ -53,7 +53,7 @@ struct NarrowArgs {
     int32_t epa_zeroed;     // 1: epa_count was zeroed by an earlier kernel of the stream (the broad phase)
     float4* det_out;        // deterministic mode: (epa_cap, 3) F, TA, TB per EPA record instead of atomics
     int32_t epa_global;     // 1: the EPA pass reads the hulls from global memory (L1) instead of staging them
-    int32_t epa_tight;      // 1: the EPA pass kernel compiled with registers capped for 7 blocks per SM
+    int32_t pad3;
     // persistent tangential history (two-pass mode): tables read at *hist_parity, written at the other
     unsigned long long* hist_keys;
     float4* hist_vals;

@@ -24,8 +24,7 @@ def bits_equal(a, b):
 @pytest.mark.parametrize("two_pass,lanes", [(True, 8), (False, 16), (True, 4 | (16 << 8) | (1 << 16)),
                                             (True, 8 | (32 << 8) | (1 << 16)), (True, 1 | (16 << 8)),
                                             (True, 1 | (8 << 8) | (1 << 16)),
-                                            (True, 1 | (16 << 8) | (1 << 16) | (1 << 17)),
-                                            (True, 4 | (32 << 8) | (1 << 17))])
+                                            (True, 1 | (32 << 8) | (1 << 16))])
 def test_pairs_vs_oracle(two_pass, lanes):
     from mwdiem_gb300.pairbench import PairScene
     ps = PairScene(6000, seed=3, pool=96, lanes=lanes, two_pass=two_pass)

@@ -199,12 +199,13 @@ def test_wall_test_band_defers_to_fp64():
     assert {p for p in want if p[0] in near and p[1] == 0}, "the band rows should include floor pairs"
 
 
-def test_deterministic_sums_equal_serial_loop():
+@pytest.mark.parametrize("lanes", [8, 1 | (16 << 8) | (1 << 16)])
+def test_deterministic_sums_equal_serial_loop(lanes):
     # deterministic mode: each particle's force and torque are summed in pair-list order, so they are
     # bit-identical to the oracle's serial loop over the same list (the reference's host build order)
     from mwdiem_gb300.sim import Simulator
     sp = dense_scene(n=700, seed=13)
-    sim = Simulator(sp, collect_collisions=True, cull_pairs=False, deterministic=True)
+    sim = Simulator(sp, collect_collisions=True, cull_pairs=False, deterministic=True, lanes=lanes)
     sim.broadphase()
     pairs = sim.pairs().cpu().numpy()
     sim.narrow_force()
@@ -267,13 +268,15 @@ def test_settling_config1_short_horizon():
     assert dq <= 1e-4
 
 
-def test_persistent_history_matches_oracle_over_steps():
+@pytest.mark.parametrize("lanes", [8, 1 | (16 << 8) | (1 << 16)])
+def test_persistent_history_matches_oracle_over_steps(lanes):
     # the history of every pair in contact carries over to the next step (the reference drops it,
     # MWDiem.py:953-966); checked step by step against the oracle's stride-4 history variant fed the
     # same pair list and a host dictionary of the histories, with bit-exact (deterministic) sums
     from mwdiem_gb300.sim import Simulator
     sp = dense_scene(n=400, seed=21, vel=0.3)
-    sim = Simulator(sp, collect_collisions=True, cull_pairs=False, deterministic=True, persistent_history=True)
+    sim = Simulator(sp, collect_collisions=True, cull_pairs=False, deterministic=True, persistent_history=True,
+                    lanes=lanes)
     ref = stepper.RefStepper(sp)
     W = sp.n_walls
     table = {}
