@@ -249,6 +249,9 @@ typedef struct {
     int32_t row_begin, wall_end, row_end, pad; /* rows [row_begin, wall_end) are walls */
     mwd_contact_params law; /* contact law of the scene */
     mwd_material mat[2];    /* derived from law by mwd_derive_material (particle, wall) */
+    float inv_cs[3];        /* optional (float)(1 / cs): cell coordinates from a float quotient away
+                               from cell boundaries (0: always the FP64 division) */
+    int32_t pad2;
 } mwd_scene;
 
 /* Particle inlet (MWDiem.py:685-714: every few steps new hulls enter the domain).  Every row is

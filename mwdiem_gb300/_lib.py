@@ -86,7 +86,8 @@ class Scene(C.Structure):
     _fields_ = [("cs", C.c_double * 3), ("box", C.c_double * 6), ("dt", C.c_double), ("wall_range", C.c_double),
                 ("nx", C.c_int64), ("ny", C.c_int64), ("key_min", C.c_int64), ("n_keys", C.c_int64),
                 ("cell_base", C.c_int64), ("row_begin", C.c_int32), ("wall_end", C.c_int32),
-                ("row_end", C.c_int32), ("pad", C.c_int32), ("law", ContactParams), ("mat", Material * 2)]
+                ("row_end", C.c_int32), ("pad", C.c_int32), ("law", ContactParams), ("mat", Material * 2),
+                ("inv_cs", C.c_float * 3), ("pad2", C.c_int32)]
 
 
 class Work(C.Structure):

@@ -251,14 +251,33 @@ struct alignas(32) dpos {
     double x, y, z, w;
 };
 
+// trunc(fl64(p / cs)), numpy's astype(int) of the FP64 quotient (MWDiem.py:813-816).  The float
+// quotient q = (float)p * (float)(1/cs) is within 1.8e-7 |q| of the double one (three roundings of
+// 2^-24), so when its fractional part is more than 2^-21 |q| away from 0 and from 1 it truncates to
+// the same integer; otherwise (and for inv = 0, |q| >= 2^23, NaN) the FP64 division decides.  FP64
+// runs at 1/64 of the FP32 rate on this GPU and the division is a long sequence of it.
+__device__ __forceinline__ int64_t cell_coord(double p, double cs, float inv)
+{
+    if (inv != 0.f) {
+        const float q = (float)p * inv;
+        const float aq = fabsf(q);
+        if (aq < 8388608.f) {
+            const float t = truncf(q);
+            const float fr = aq - fabsf(t);  // exact: |t| <= aq < |t| + 1
+            const float band = aq * 4.76837158203125e-7f;
+            if (fr > band && fr < 1.f - band) return (int64_t)t;
+        }
+    }
+    return (int64_t)(p / cs);
+}
+
 __device__ __forceinline__ int64_t row_key(const BroadArgs& a, const mwd_scene& sc, int r)
 {
     if (a.keys) return a.keys[r];
     const dpos p = reinterpret_cast<const dpos*>(a.pos)[r];
-    // numpy astype(int): truncation toward zero of the FP64 quotient (MWDiem.py:813-816)
-    const int64_t xc = (int64_t)(p.x / sc.cs[0]);
-    const int64_t yc = (int64_t)(p.y / sc.cs[1]);
-    const int64_t zc = (int64_t)(p.z / sc.cs[2]);
+    const int64_t xc = cell_coord(p.x, sc.cs[0], sc.inv_cs[0]);
+    const int64_t yc = cell_coord(p.y, sc.cs[1], sc.inv_cs[1]);
+    const int64_t zc = cell_coord(p.z, sc.cs[2], sc.inv_cs[2]);
     return xc + yc * sc.nx + zc * sc.nx * sc.ny;
 }
 
@@ -402,14 +421,16 @@ struct WallStage {
 
 // every candidate of the row at sorted position t (row r, cell g), passed to sink(A, B).
 // ws: optional float copies of the row's scene walls for the wall-distance test.
+// part: -1 the whole walk; 0 the walls and the later members of the row's own cell; 1..7 the
+// members of forward neighbour cell part - 1 (the eight parts together are the whole walk)
 template <class Sink>
 __device__ __forceinline__ void walk_pairs(const BroadArgs& a, int t, int r, int g, const mwd_scene& sc, int scene,
-                                           const WallStage* ws, Sink&& sink)
+                                           const WallStage* ws, Sink&& sink, int part = -1)
 {
     const bool cull = a.cull && a.sorted_pos;
     const float4 me = a.sorted_pos ? a.sorted_pos[t] : make_float4(0.f, 0.f, 0.f, 0.f);
     // wall candidates (MWDiem.py:808-811): pair [particle, wall] when |n . (p - c)| < wall_range (FP64)
-    if (a.walls) {
+    if (a.walls && part <= 0) {
         if (ws && ws->scene == scene && a.sorted_pos) {
             // FP32 test with a margin above its rounding error (inputs rounded to float, three products
             // and two sums: < 6 u |n|_1 sum_i (|p_i| + |c_i|) with u = 2^-24); inside the margin band,
@@ -455,12 +476,23 @@ __device__ __forceinline__ void walk_pairs(const BroadArgs& a, int t, int r, int
         sink(r, B);
     };
     // later members of the same cell, in set order
-    const int ce = a.cell_start[g + 1];
-    for (int j = t + 1; j < ce; ++j) put(a.sorted[j], j);
+    if (part <= 0) {
+        const int ce = a.cell_start[g + 1];
+        for (int j = t + 1; j < ce; ++j) put(a.sorted[j], j);
+    }
+    if (part == 0) return;
     // forward neighbours
     const int64_t local = (int64_t)g - sc.cell_base;
     const int64_t nx = sc.nx, nxy = sc.nx * sc.ny;
     const int64_t offs[7] = {1, nx, nxy, nxy + 1, nxy + 1 + nx, nxy + nx, nx + 1};
+    if (part > 0) {
+        const int64_t l2 = local + offs[part - 1];
+        if (l2 < 0 || l2 >= sc.n_keys) return;
+        const int g2 = (int)(sc.cell_base + l2);
+        const int e2 = a.cell_start[g2 + 1];
+        for (int j = a.cell_start[g2]; j < e2; ++j) put(a.sorted[j], j);
+        return;
+    }
     // the 7 neighbour ranges are loaded first (independent loads), then walked
     int rs[7], re[7];
 #pragma unroll
@@ -509,10 +541,13 @@ __global__ void pairs_kernel(BroadArgs a)
 }
 
 constexpr int APPEND_THREADS = 128;
-constexpr int APPEND_KEEP = 8;  // pairs a thread keeps from its walk; rows with more walk again
+constexpr int APPEND_KEEP = 8;   // pairs a thread keeps from its walk; threads with more walk again
+constexpr int APPEND_PARTS = 8;  // threads per row: walls + own cell, and each forward neighbour cell
 
 // one walk (the first APPEND_KEEP pairs kept in shared memory), reserve (one atomic per warp on
-// n_pairs, zeroed by assign_kernel), write
+// n_pairs, zeroed by assign_kernel), write.  Each row's walk is split over APPEND_PARTS threads (its
+// own cell and walls, and one per forward neighbour), so the chain of dependent loads per thread is
+// short; the list order is arbitrary anyway in this mode.
 __global__ void __launch_bounds__(APPEND_THREADS) pairs_append_kernel(BroadArgs a)
 {
     pdl_wait();
@@ -520,15 +555,16 @@ __global__ void __launch_bounds__(APPEND_THREADS) pairs_append_kernel(BroadArgs 
     __shared__ int2 keep[APPEND_KEEP][APPEND_THREADS];
     __shared__ float4 s_wc[WALL_STAGE], s_wn[WALL_STAGE];
     __shared__ int s_scene, s_nw;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t == 0) *a.n_crowded = 0;  // consumed by the crowded-cell pass, which ran before
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = tid / APPEND_PARTS, part = tid % APPEND_PARTS;
+    if (tid == 0) *a.n_crowded = 0;  // consumed by the crowded-cell pass, which ran before
     const int n_sorted = a.cell_start[a.total_cells];
     const bool live = t < n_sorted;
     // the walls of the scene of the block's first row, as floats
     if (threadIdx.x == 0) {
         s_scene = -1;
         s_nw = 0;
-        const int t0 = blockIdx.x * blockDim.x;
+        const int t0 = blockIdx.x * blockDim.x / APPEND_PARTS;
         if (a.walls && a.sorted_pos && t0 < n_sorted) {
             const int sc0 = scene_of(a, a.sorted[t0]);
             const mwd_scene& sc = a.scenes[sc0];
@@ -560,7 +596,7 @@ __global__ void __launch_bounds__(APPEND_THREADS) pairs_append_kernel(BroadArgs 
         walk_pairs(a, t, r, g, *sc, scene, &ws, [&](int A, int B) {
             if (c < APPEND_KEEP) keep[c][threadIdx.x] = make_int2(A, B);
             ++c;
-        });
+        }, part);
     }
     const int lane = threadIdx.x & 31;
     int inc = c;
@@ -586,7 +622,7 @@ __global__ void __launch_bounds__(APPEND_THREADS) pairs_append_kernel(BroadArgs 
         walk_pairs(a, t, r, g, *sc, scene, &ws, [&](int A, int B) {
             if (i >= APPEND_KEEP && out + i < cap) pairs[out + i] = make_int2(A, B);
             ++i;
-        });
+        }, part);
     }
 }
 
@@ -685,11 +721,13 @@ int launch_broad(const BroadArgs& a, cudaStream_t s)
     if (rc) return rc;
     MWD_CUDA(launch_pdl(scatter_kernel, blocks(rows, T), T, 0, s, a));
     MWD_CUDA(launch_pdl(order_kernel, blocks(rows, T), T, 0, s, a));
-    MWD_CUDA(launch_pdl(order_crowded_kernel,
-                        (unsigned)(a.crowded_cap < 1024 ? (a.crowded_cap > 0 ? a.crowded_cap : 1) : 1024), 32, 0, s, a));
+    // one warp per crowded cell; usually there are none, so a small grid that strides over them
+    const int64_t cg = a.crowded_cap < num_sms() ? a.crowded_cap : num_sms();
+    MWD_CUDA(launch_pdl(order_crowded_kernel, (unsigned)(cg > 0 ? cg : 1), 32, 0, s, a));
     // rows that have a cell are at most `rows`; threads past cell_start[total] exit
     if (a.append) {
-        MWD_CUDA(launch_pdl(pairs_append_kernel, blocks(rows, APPEND_THREADS), APPEND_THREADS, 0, s, a));
+        MWD_CUDA(launch_pdl(pairs_append_kernel, blocks(rows * APPEND_PARTS, APPEND_THREADS), APPEND_THREADS, 0, s,
+                            a));
         MWD_CUDA(cudaGetLastError());
         return MWD_OK;
     }

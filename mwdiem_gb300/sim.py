@@ -256,6 +256,8 @@ class Simulator:
             for a in range(6):
                 sc.box[a] = float(box[a])
             sc.dt = float(sp.dt)
+            for k in range(3):
+                sc.inv_cs[k] = float(np.float32(1.0 / cs[k]))
             sc.wall_range = 6.0 * float(sp.max_particlesize)
             nx, ny = int(ncell[0]), int(ncell[1])
             sc.nx, sc.ny = nx, ny

@@ -1,8 +1,9 @@
-"""The narrow phase decides two of the reference's double-precision tests in FP32 (FP64 is slow on
-this GPU): CorrectFlat's +-1e-6 window (gpu_fine_contact_detection.cu:256-268) and the EPA's relative
-1e-5 convergence test (.cu:439).  These restate the kernel's filters (narrow.cu within_1e6,
-epa_converged) in numpy float32 arithmetic, which rounds as the kernel does (no fused multiply-add),
-and check that they give the double tests' answers on random and adversarial inputs."""
+"""Three of the reference's double-precision computations are decided in FP32 on the device (FP64
+is slow on this GPU): CorrectFlat's +-1e-6 window (gpu_fine_contact_detection.cu:256-268), the EPA's
+relative 1e-5 convergence test (.cu:439) and the cell coordinate trunc(p / cs) (MWDiem.py:813-816).
+These restate the kernels' filters (narrow.cu within_1e6, epa_converged; broad.cu cell_coord) in
+numpy float32 arithmetic, which rounds as the kernels do (no fused multiply-add), and check that they
+give the double computations' answers on random and adversarial inputs."""
 import numpy as np
 
 f32 = np.float32
@@ -86,3 +87,30 @@ def test_epa_convergence_filter_matches_double():
     assert np.array_equal(got, epa_converged_ref(x, p))
     # the FP64 fallback is rare even for p spread within a few 1e-5 of x
     assert slow[:n].mean() < 0.03
+
+
+def cell_coord(p, cs):
+    """broad.cu cell_coord: the float quotient away from integers, else the double division."""
+    inv = f32(1.0 / cs)
+    q = p.astype(f32) * inv
+    aq = np.abs(q)
+    with np.errstate(invalid="ignore"):
+        t = np.trunc(q)
+        fr = aq - np.abs(t)
+        band = aq * f32(4.76837158203125e-7)
+        fast = (aq < f32(8388608.0)) & (fr > band) & (fr < f32(1.0) - band)
+        ref = np.trunc(p / cs)
+    return np.where(fast, t.astype(np.float64), ref), fast
+
+
+def test_cell_coordinate_filter_matches_double():
+    rng = np.random.default_rng(3)
+    for cs in (2.4444444444444446, 2.4212962962962963, 1.0, 0.3, 7.123456789):
+        p = np.concatenate([rng.uniform(-300, 300, 200000), rng.normal(0, 5, 50000)])
+        # centres a few ulps either side of every cell boundary in range
+        k = np.arange(-120, 121)
+        edge = (k * cs)[:, None] + np.array([-2, -1, 0, 1, 2])[None, :] * np.spacing(np.abs(k * cs) + 1.0)[:, None]
+        p = np.concatenate([p, edge.ravel(), [0.0, -0.0, 1e-300, -1e-300]])
+        got, fast = cell_coord(p, cs)
+        assert np.array_equal(got, np.trunc(p / cs)), cs
+        assert fast[:200000].mean() > 0.999
