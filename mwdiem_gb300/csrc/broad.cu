@@ -305,12 +305,22 @@ __global__ void assign_kernel(BroadArgs a)
     const int g = (int)(sc.cell_base + local);
     a.cell_of[r] = g;
     atomicAdd(a.cell_count + g, 1);
+    if (a.tile_sums) {
+        // one atomic per tile per warp (consecutive rows mostly share a tile)
+        const int tile = g / SCAN_TILE;
+        const unsigned peers = __match_any_sync(__activemask(), tile);
+        if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(a.tile_sums + tile, __popc(peers));
+    }
 }
 
 __global__ void scatter_kernel(BroadArgs a)
 {
     pdl_wait();
     pdl_launch_dependents();
+    if (a.tile_sums) {  // read by the cell scan, which has finished: zero for the next broad phase
+        const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (i < (a.total_cells + SCAN_TILE - 1) / SCAN_TILE) a.tile_sums[i] = 0;
+    }
     const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= a.row_hi) return;
     const int g = a.cell_of[r];
@@ -689,7 +699,10 @@ inline unsigned blocks(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
 
-int64_t scan_tmp_ints(int64_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 2; }
+// block totals of a scan of n elements, then (device-resident broad phase) as many persistent
+// per-tile cell counts
+int64_t scan_tmp_ints(int64_t n) { return 2 * ((n + SCAN_TILE - 1) / SCAN_TILE + 2); }
+int64_t scan_tile_sums_offset(int64_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 2; }
 
 int launch_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* tmp, int64_t* total_out, int64_t cap,
                 uint32_t* status, uint32_t overflow_bit, cudaStream_t s)
@@ -717,8 +730,17 @@ int launch_broad(const BroadArgs& a, cudaStream_t s)
         return MWD_OK;
     }
     MWD_CUDA(launch_pdl(assign_kernel, blocks(rows, T), T, 0, s, a));
-    int rc = launch_scan(a.cell_count, a.total_cells, a.cell_start, a.scan_tmp, nullptr, INT64_MAX, nullptr, 0, s);
-    if (rc) return rc;
+    int rc = MWD_OK;
+    if (a.tile_sums && a.total_cells > SCAN_SMALL_MAX) {
+        // the tile totals were added up by assign_kernel: only the final pass of the scan remains
+        const int nb = (int)((a.total_cells + SCAN_TILE - 1) / SCAN_TILE);
+        MWD_CUDA(launch_pdl(scan_final_kernel, nb, SCAN_THREADS, 0, s, (const int32_t*)a.cell_count, a.total_cells,
+                            (const int32_t*)a.tile_sums, a.cell_start, nb, (int64_t*)nullptr, (int64_t)INT64_MAX,
+                            (uint32_t*)nullptr, 0u));
+    } else {
+        rc = launch_scan(a.cell_count, a.total_cells, a.cell_start, a.scan_tmp, nullptr, INT64_MAX, nullptr, 0, s);
+        if (rc) return rc;
+    }
     MWD_CUDA(launch_pdl(scatter_kernel, blocks(rows, T), T, 0, s, a));
     MWD_CUDA(launch_pdl(order_kernel, blocks(rows, T), T, 0, s, a));
     // one warp per crowded cell; usually there are none, so a small grid that strides over them

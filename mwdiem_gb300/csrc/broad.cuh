@@ -35,9 +35,12 @@ struct BroadArgs {
     uint32_t* status;
     int64_t total_cells;
     int64_t pair_cap;
+    int32_t* tile_sums;          // optional: per-scan-tile cell counts, added to by assign_kernel, read by
+                                 // the cell scan (no reduce pass) and zeroed by scatter_kernel
 };
 
 int64_t scan_tmp_ints(int64_t n);
+int64_t scan_tile_sums_offset(int64_t n);  // where the persistent cell-tile counts start in scan_tmp
 int launch_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* tmp, int64_t* total_out, int64_t cap,
                 uint32_t* status, uint32_t overflow_bit, cudaStream_t s);
 int launch_broad(const BroadArgs& a, cudaStream_t s);

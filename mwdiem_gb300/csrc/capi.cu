@@ -416,6 +416,13 @@ int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_s
     a.epa_count = work->epa_rec ? work->epa_count : nullptr;
     a.sorted_pos = reinterpret_cast<float4*>(work->sorted_pos);
     a.sorted_cell = work->sorted_cell;
+    // scan_tmp holds mwd_scan_tmp_ints(max(total_cells, n) + 1) ints: its second half keeps the
+    // per-tile cell counts the assign pass adds up (zero on entry and on exit)
+    {
+        const int64_t rows = (int64_t)st->n;
+        const int64_t m = (work->total_cells > rows ? work->total_cells : rows) + 1;
+        a.tile_sums = work->scan_tmp + scan_tile_sums_offset(m);
+    }
     return launch_broad(a, reinterpret_cast<cudaStream_t>(stream));
 }
 
