@@ -56,9 +56,11 @@ class host_prints_to_stderr:
 METRIC = "particle-steps/s"
 WINDOW_STEPS = 500  # the pour configuration runs 500 steps
 # DRAM bytes (read + write) of one GJK-pass and one EPA-pass launch of this step, from the ncu capture
-# summarised in profiles/step_kernels_pour20k.md (5.205 MB + 0.151 MB; writes stay in L2)
-NARROW_DRAM_BYTES_PER_LAUNCH = 5.204992e6 + 0.151040e6
-KERNELS_PER_STEP = 11  # broad phase 7 (assign, 2 scan, scatter, order, crowded, append) + GJK pass + EPA pass + integrate rows + vertices
+# summarised in profiles/step_kernels_pour20k.md (5.180 MB + 0.163 MB; writes stay in L2)
+NARROW_DRAM_BYTES_PER_LAUNCH = 5.179648e6 + 0.163328e6
+# broad phase 6 (assign, cell scan, scatter, order, crowded cells, append) + GJK pass + EPA pass
+# + integrator rows + vertices
+KERNELS_PER_STEP = 10
 
 
 def parse():
@@ -90,6 +92,8 @@ def parse():
     ap.add_argument("--contact-point", default="midpoint", choices=["reference", "midpoint"],
                     help="calibration's torque-arm contact point: the reference's (cpA - cpB)/2 spins particles "
                          "far from the origin up until the 5,000-step pour flies apart, so the midpoint is the default")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="only the batched step (config 4) with --lanes (no tuning, no sequential comparison)")
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--batch-total", type=int, default=2_000_000)
     return ap.parse_args()
@@ -238,6 +242,9 @@ def main():
         return 0
     if args.batch_compare:
         print(json.dumps({"batch": batch_compare(args)}), flush=True)
+        return 0
+    if args.batch_only:
+        print(json.dumps({"batch_only": batch_only(args)}), flush=True)
         return 0
     if args.calibration:
         print(json.dumps({"calibration": calibration(args)}), flush=True)
@@ -394,7 +401,7 @@ def breakdown(sim, V, flush, reps=10):
                 "traffic": NARROW_DRAM_BYTES_PER_LAUNCH,
                 "traffic_source": "profiles/step_kernels_pour20k.md (ncu dram__bytes_read + write, one launch each)",
                 "note": "latency-bound: ~13k candidate pairs, each a chain of dependent support queries; the "
-                        "GJK pass issues on ~44% of cycles, the EPA pass waits on its few longest pairs",
+                        "GJK pass issues on ~40% of cycles, the EPA pass waits on its few longest pairs",
                 "peak_source": "measured in this run (mwd_probe_fp32: FMUL+FADD chains, no FMA)"}
     elif dom == "integrate":
         hbm = pk.get("hbm_gbs", 6800.0)
@@ -407,7 +414,7 @@ def breakdown(sim, V, flush, reps=10):
         n, P = sim.n, sim.n_pairs()
         bbytes = n * (32 + 4 + 4 + 4 + 4 + 4 + 8) + sim.total_cells * 12 + P * (8 + 8 + 8)
         a = bbytes / (ms["broad"] * 1e-3) / 1e9
-        roof = {"kernel": "broad phase (7 kernels)", "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s",
+        roof = {"kernel": "broad phase (6 kernels)", "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s",
                 "frac": a / hbm, "traffic": None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in pk else "fallback 6800"}
     return out, roof
@@ -610,6 +617,29 @@ def settling(args, steps=2000, cpu_seconds=20.0):
                   "dtype": "f32 state, f64 centres", "graph_steps": per, "status": sim.status(),
                   "sample": f"{steps} steps after 1 + {3 * per} warm-up steps"}
     return out
+
+
+def batch_only(args):
+    """Config 4's batched step alone: all scenes in one state, the step captured in one CUDA graph,
+    --lanes fixed, --warmup then --steps replays timed with CUDA events."""
+    import torch
+    from mwdiem_gb300 import scene
+    from mwdiem_gb300.sim import Simulator
+    specs = scene.batched_scenes(n_scenes=args.batch_scenes, total=args.batch_total, seed=0)
+    n_total = sum(sp.n_particles for sp in specs)
+    sim = Simulator(specs, lanes=args.lanes)
+    sim.capture(1)
+    sim.replay(max(1, args.warmup))
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.replay(max(1, args.steps))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / max(1, args.steps)
+    return {"scenes": len(specs), "particles": int(n_total), "lanes": args.lanes, "ms_per_step": ms,
+            "particle_steps_per_s": n_total / (ms * 1e-3), "status": sim.status()}
 
 
 def calibration(args):
