@@ -555,9 +555,11 @@ constexpr int APPEND_KEEP = 8;   // pairs a thread keeps from its walk; threads 
 constexpr int APPEND_PARTS = 8;  // threads per row: walls + own cell, and each forward neighbour cell
 
 // one walk (the first APPEND_KEEP pairs kept in shared memory), reserve (one atomic per warp on
-// n_pairs, zeroed by assign_kernel), write.  Each row's walk is split over APPEND_PARTS threads (its
-// own cell and walls, and one per forward neighbour), so the chain of dependent loads per thread is
-// short; the list order is arbitrary anyway in this mode.
+// n_pairs, zeroed by assign_kernel), write.  With walk_parts = APPEND_PARTS each row's walk is split
+// over that many threads (its own cell and walls, and one per forward neighbour), so the chain of
+// dependent loads per thread is short (a 20k-row step: 72.9 -> 68.7 us); with many rows one thread
+// per row does less redundant work (2M rows: 1.33 -> 0.99 ms).  The list order is arbitrary anyway
+// in this mode.
 __global__ void __launch_bounds__(APPEND_THREADS) pairs_append_kernel(BroadArgs a)
 {
     pdl_wait();
@@ -566,7 +568,8 @@ __global__ void __launch_bounds__(APPEND_THREADS) pairs_append_kernel(BroadArgs 
     __shared__ float4 s_wc[WALL_STAGE], s_wn[WALL_STAGE];
     __shared__ int s_scene, s_nw;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int t = tid / APPEND_PARTS, part = tid % APPEND_PARTS;
+    const int t = a.walk_parts > 1 ? tid / APPEND_PARTS : tid;
+    const int part = a.walk_parts > 1 ? tid % APPEND_PARTS : -1;
     if (tid == 0) *a.n_crowded = 0;  // consumed by the crowded-cell pass, which ran before
     const int n_sorted = a.cell_start[a.total_cells];
     const bool live = t < n_sorted;
@@ -574,7 +577,7 @@ __global__ void __launch_bounds__(APPEND_THREADS) pairs_append_kernel(BroadArgs 
     if (threadIdx.x == 0) {
         s_scene = -1;
         s_nw = 0;
-        const int t0 = blockIdx.x * blockDim.x / APPEND_PARTS;
+        const int t0 = blockIdx.x * blockDim.x / (a.walk_parts > 1 ? APPEND_PARTS : 1);
         if (a.walls && a.sorted_pos && t0 < n_sorted) {
             const int sc0 = scene_of(a, a.sorted[t0]);
             const mwd_scene& sc = a.scenes[sc0];
@@ -748,8 +751,13 @@ int launch_broad(const BroadArgs& a, cudaStream_t s)
     MWD_CUDA(launch_pdl(order_crowded_kernel, (unsigned)(cg > 0 ? cg : 1), 32, 0, s, a));
     // rows that have a cell are at most `rows`; threads past cell_start[total] exit
     if (a.append) {
-        MWD_CUDA(launch_pdl(pairs_append_kernel, blocks(rows * APPEND_PARTS, APPEND_THREADS), APPEND_THREADS, 0, s,
-                            a));
+        // split each row's walk over APPEND_PARTS threads while the rows alone leave the GPU short of
+        // threads (a latency-bound step); with many rows one thread per row does less redundant work
+        BroadArgs b = a;
+        const int64_t resident = (int64_t)num_sms() * 2048;
+        b.walk_parts = rows * APPEND_PARTS <= 4 * resident ? APPEND_PARTS : 1;
+        MWD_CUDA(launch_pdl(pairs_append_kernel, blocks(rows * b.walk_parts, APPEND_THREADS), APPEND_THREADS, 0, s,
+                            b));
         MWD_CUDA(cudaGetLastError());
         return MWD_OK;
     }
