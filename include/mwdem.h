@@ -324,7 +324,9 @@ typedef struct {
 /* Scratch bytes of the deterministic accumulation for n rows and epa_cap contacts. */
 int64_t mwd_det_scratch_bytes(int32_t n, int64_t epa_cap);
 
-/* Scratch ints the device-wide scans need for arrays of n elements. */
+/* Scratch ints the device-wide scans need for arrays of n elements: the block totals of a scan, and
+ * as many again for the per-tile cell counts the device-resident broad phase keeps between its
+ * assign pass and its cell scan (zero on entry and on exit; allocate zeroed). */
 int64_t mwd_scan_tmp_ints(int64_t n);
 
 /* One broad phase over all scenes (rows of every scene; walls excluded from the cell hash). */
