@@ -58,9 +58,9 @@ WINDOW_STEPS = 500  # the pour configuration runs 500 steps
 # DRAM bytes (read + write) of one GJK-pass and one EPA-pass launch of this step, from the ncu capture
 # summarised in profiles/step_kernels_pour20k.md (5.180 MB + 0.163 MB; writes stay in L2)
 NARROW_DRAM_BYTES_PER_LAUNCH = 5.179648e6 + 0.163328e6
-# broad phase 6 (assign, cell scan, scatter, order, crowded cells, append) + GJK pass + EPA pass
-# + integrator rows + vertices
-KERNELS_PER_STEP = 10
+# broad phase 5 (assign, cell scan, scatter, order, append) + GJK pass + EPA pass + integrator rows
+# + vertices
+KERNELS_PER_STEP = 9
 
 
 def parse():
@@ -414,7 +414,7 @@ def breakdown(sim, V, flush, reps=10):
         n, P = sim.n, sim.n_pairs()
         bbytes = n * (32 + 4 + 4 + 4 + 4 + 4 + 8) + sim.total_cells * 12 + P * (8 + 8 + 8)
         a = bbytes / (ms["broad"] * 1e-3) / 1e9
-        roof = {"kernel": "broad phase (6 kernels)", "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s",
+        roof = {"kernel": "broad phase (5 kernels)", "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s",
                 "frac": a / hbm, "traffic": None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in pk else "fallback 6800"}
     return out, roof

@@ -284,9 +284,6 @@ typedef struct {
     int64_t* n_pairs;      /* (1,) candidate count of the last broad phase */
     uint32_t* status;      /* (1,) status word */
     int32_t* collision;    /* (pair_cap,) optional contact flags (NULL to skip) */
-    int32_t* crowded;      /* (crowded_cap,) cells with more than 32 members (set order by a warp) */
-    int32_t* n_crowded;    /* (1,) zero on entry, left zero on exit */
-    int64_t crowded_cap;   /* n / 33 + 1 is always enough */
     uint64_t* work_counters; /* optional (3,), added to by the narrow phase: vertex dot products of the
                               support queries, EPA faces created, support queries (NULL: not counted) */
     int32_t* epa_count;    /* (1,) two-pass narrow phase: pairs found in contact by the GJK pass */

@@ -92,8 +92,8 @@ class Scene(C.Structure):
 
 class Work(C.Structure):
     _fields_ = [(n, _P) for n in ("cell_count", "cell_start", "cell_of", "sorted", "pair_count", "pairs",
-                                  "scan_tmp", "n_pairs", "status", "collision", "crowded", "n_crowded")] + \
-               [("crowded_cap", C.c_int64), ("work_counters", _P), ("epa_count", _P), ("epa_rec", _P),
+                                  "scan_tmp", "n_pairs", "status", "collision")] + \
+               [("work_counters", _P), ("epa_count", _P), ("epa_rec", _P),
                 ("epa_cap", C.c_int64), ("sorted_pos", _P), ("sorted_cell", _P), ("cull_pairs", C.c_int32),
                 ("pad", C.c_int32), ("total_cells", C.c_int64),
                 ("pair_cap", C.c_int64), ("face_ids", _P), ("deterministic", C.c_int32),

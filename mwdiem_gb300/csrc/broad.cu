@@ -340,28 +340,22 @@ __device__ __forceinline__ void place(const BroadArgs& a, int i, int v, int g)
     }
 }
 
-__global__ void order_kernel(BroadArgs a)
+// one row of the order pass: singletons placed, small cells ordered by their smallest member's thread;
+// returns the cell to the caller when it is crowded (its smallest member's thread), else -1
+__device__ __forceinline__ int order_row(const BroadArgs& a, int r)
 {
-    pdl_wait();
-    pdl_launch_dependents();
-    const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= a.row_hi) return;
+    if (r >= a.row_hi) return -1;
     const int g = a.cell_of[r];
-    if (g < 0) return;
+    if (g < 0) return -1;
     const int s = a.cell_start[g], e = a.cell_start[g + 1];
     const int k = e - s;
     if (k == 1) {
         place(a, s, r, g);
-        return;
+        return -1;
     }
     for (int j = s; j < e; ++j)
-        if (a.scatter_out[j] < r) return;  // the smallest id of the cell orders it
-    if (k > SMALL_CELL) {
-        const int idx = atomicAdd(a.n_crowded, 1);
-        if (idx < a.crowded_cap) a.crowded[idx] = g;
-        else set_status(a.status, MWD_ST_CELL_CROWDED);
-        return;
-    }
+        if (a.scatter_out[j] < r) return -1;  // the smallest id of the cell orders it
+    if (k > SMALL_CELL) return g;
     int m[SMALL_CELL];
     for (int j = 0; j < k; ++j) {
         int v = a.scatter_out[s + j];
@@ -378,21 +372,32 @@ __global__ void order_kernel(BroadArgs a)
     const int base = a.info ? a.scenes[scene_of(a, r)].row_begin : 0;
     pyset_order<SMALL_TAB>(m, k, o, tab, used, tmp, used2, base);
     for (int j = 0; j < k; ++j) place(a, s + j, o[j], g);
+    return -1;
 }
 
-// one warp per crowded cell: members ranked by id in parallel, then lane 0 replays the set inserts
-__global__ void __launch_bounds__(32) order_crowded_kernel(BroadArgs a)
+// the order pass: every row of the block, then the block's crowded cells (more than SMALL_CELL
+// members, usually none) by its first warp -- members ranked by id in parallel, lane 0 replaying the
+// set inserts with the table in shared memory
+constexpr int ORDER_THREADS = 128;
+__global__ void __launch_bounds__(ORDER_THREADS) order_kernel(BroadArgs a)
 {
     pdl_wait();
     pdl_launch_dependents();
+    __shared__ int s_crowd[ORDER_THREADS];
+    __shared__ int s_nc;
+    if (threadIdx.x == 0) s_nc = 0;
+    __syncthreads();
+    const int g0 = order_row(a, a.row_lo + blockIdx.x * blockDim.x + threadIdx.x);
+    if (g0 >= 0) s_crowd[atomicAdd(&s_nc, 1)] = g0;
+    __syncthreads();
+    const int nc = s_nc;
+    if (nc == 0 || threadIdx.x >= 32) return;
     __shared__ int m[BIG_CELL];
     __shared__ int o[BIG_CELL];
     __shared__ int tab[BIG_TAB], tmp[BIG_TAB];
     __shared__ unsigned char used[BIG_TAB], used2[BIG_TAB];
-    const int64_t nc = *a.n_crowded;
-    const int n = (int)(nc < a.crowded_cap ? nc : a.crowded_cap);
-    for (int c = blockIdx.x; c < n; c += gridDim.x) {
-        const int g = a.crowded[c];
+    for (int c = 0; c < nc; ++c) {
+        const int g = s_crowd[c];
         const int s = a.cell_start[g], e = a.cell_start[g + 1];
         const int k = e - s;
         if (k > BIG_CELL) {
@@ -525,7 +530,6 @@ __global__ void pairs_kernel(BroadArgs a)
     pdl_wait();
     pdl_launch_dependents();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!EMIT && t == 0) *a.n_crowded = 0;  // consumed by the crowded-cell pass, which ran before
     const int n_sorted = a.cell_start[a.total_cells];
     if (t >= n_sorted) {
         if (!EMIT && t < a.row_hi - a.row_lo) a.pair_count[t] = 0;
@@ -570,7 +574,6 @@ __global__ void __launch_bounds__(APPEND_THREADS) pairs_append_kernel(BroadArgs 
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int t = a.walk_parts > 1 ? tid / APPEND_PARTS : tid;
     const int part = a.walk_parts > 1 ? tid % APPEND_PARTS : -1;
-    if (tid == 0) *a.n_crowded = 0;  // consumed by the crowded-cell pass, which ran before
     const int n_sorted = a.cell_start[a.total_cells];
     const bool live = t < n_sorted;
     // the walls of the scene of the block's first row, as floats
@@ -745,10 +748,7 @@ int launch_broad(const BroadArgs& a, cudaStream_t s)
         if (rc) return rc;
     }
     MWD_CUDA(launch_pdl(scatter_kernel, blocks(rows, T), T, 0, s, a));
-    MWD_CUDA(launch_pdl(order_kernel, blocks(rows, T), T, 0, s, a));
-    // one warp per crowded cell; usually there are none, so a small grid that strides over them
-    const int64_t cg = a.crowded_cap < num_sms() ? a.crowded_cap : num_sms();
-    MWD_CUDA(launch_pdl(order_crowded_kernel, (unsigned)(cg > 0 ? cg : 1), 32, 0, s, a));
+    MWD_CUDA(launch_pdl(order_kernel, blocks(rows, ORDER_THREADS), ORDER_THREADS, 0, s, a));
     // rows that have a cell are at most `rows`; threads past cell_start[total] exit
     if (a.append) {
         // split each row's walk over APPEND_PARTS threads while the rows alone leave the GPU short of

@@ -26,9 +26,6 @@ struct BroadArgs {
     int32_t* sorted_cell;        // (n,) with sorted_pos: their cells
     int32_t* pair_count;         // (rows+1,)
     int32_t* scan_tmp;
-    int32_t* crowded;            // (crowded_cap,) cells with more than 32 members, this step
-    int32_t* n_crowded;          // (1,) zero on entry and on exit
-    int64_t crowded_cap;
     int32_t* pairs;              // (pair_cap,2)
     int64_t* n_pairs;
     int32_t* epa_count;          // optional: zeroed by assign_kernel for the narrow phase that follows

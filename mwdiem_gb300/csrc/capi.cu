@@ -337,8 +337,6 @@ int mwd_linked_cell_hash(int32_t n_lo, int32_t n_hi, const int64_t* keys, int64_
     size_t o_sorted = c.take<int32_t>(n_hi);
     size_t o_pc = c.take<int32_t>(rows + 1);
     size_t o_tmp = c.take<int32_t>(scan_tmp_ints(R > rows ? R + 1 : rows + 1));
-    const int64_t crowded_cap = rows / 33 + 1;
-    size_t o_crowd = c.take<int32_t>(crowded_cap + 1);
     rc = scratch(c.off, &base);
     if (rc) return rc;
     char* b = (char*)base;
@@ -350,7 +348,6 @@ int mwd_linked_cell_hash(int32_t n_lo, int32_t n_hi, const int64_t* keys, int64_
     sc.cell_base = 0;
     MWD_CUDA(cudaMemcpyAsync(b + o_scene, &sc, sizeof(sc), cudaMemcpyHostToDevice, s));
     MWD_CUDA(cudaMemsetAsync(b + o_count, 0, R * sizeof(int32_t), s));
-    MWD_CUDA(cudaMemsetAsync(b + o_crowd, 0, sizeof(int32_t), s));
     BroadArgs a = {};
     a.row_lo = n_lo;
     a.row_hi = n_hi;
@@ -364,9 +361,6 @@ int mwd_linked_cell_hash(int32_t n_lo, int32_t n_hi, const int64_t* keys, int64_
     a.sorted = reinterpret_cast<int32_t*>(b + o_sorted);
     a.pair_count = reinterpret_cast<int32_t*>(b + o_pc);
     a.scan_tmp = reinterpret_cast<int32_t*>(b + o_tmp);
-    a.crowded = reinterpret_cast<int32_t*>(b + o_crowd) + 1;
-    a.n_crowded = reinterpret_cast<int32_t*>(b + o_crowd);
-    a.crowded_cap = crowded_cap;
     a.pairs = pairs;
     a.n_pairs = n_out;
     a.status = status;
@@ -400,9 +394,6 @@ int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_s
     a.cell_start = work->cell_start;
     a.cell_of = work->cell_of;
     a.scatter_out = work->pair_count;  // free until the count pass
-    a.crowded = work->crowded;
-    a.n_crowded = work->n_crowded;
-    a.crowded_cap = work->crowded_cap;
     a.sorted = work->sorted;
     a.pair_count = work->pair_count;
     a.scan_tmp = work->scan_tmp;

@@ -299,17 +299,12 @@ class Simulator:
         w["n_pairs"] = torch.zeros(1, dtype=torch.int64, device=self.device)
         w["status"] = torch.zeros(1, **i32)
         w["collision"] = torch.zeros(cap, **i32) if collect_collisions else None
-        crowded_cap = n // 33 + 1
-        w["crowded"] = torch.zeros(crowded_cap + 1, **i32)
         self.w = w
         wk = Work()
         for k in ("cell_count", "cell_start", "cell_of", "sorted", "pair_count", "pairs", "scan_tmp", "n_pairs",
                   "status"):
             setattr(wk, k, w[k].data_ptr())
         wk.collision = w["collision"].data_ptr() if w["collision"] is not None else None
-        wk.n_crowded = w["crowded"].data_ptr()
-        wk.crowded = w["crowded"].data_ptr() + 4
-        wk.crowded_cap = crowded_cap
         w["work_counters"] = torch.zeros(3, dtype=torch.int64, device=self.device)
         wk.work_counters = None
         if self.two_pass:
