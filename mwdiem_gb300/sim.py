@@ -234,6 +234,19 @@ class Simulator:
         # the integrator's vertex pass: one thread per vertex, through each row's transform
         t["vert_owner"] = owner.to(torch.int32)
         t["xform"] = torch.zeros((n, 16), **f32)
+        # the state a step updates, in one contiguous buffer: a host round trip of it is then one copy
+        # each way (step_host)
+        nbytes = sum(t[k].numel() * t[k].element_size() for k in self.MUTABLE)
+        buf = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        off = 0
+        for k in self.MUTABLE:
+            v = t[k]
+            b = v.numel() * v.element_size()
+            view = buf[off:off + b].view(v.dtype).view(v.shape)
+            view.copy_(v)
+            t[k] = view
+            off += b
+        self.mutable = buf
         self.t = t
         st = State()
         for k in _STATE_F64 + _STATE_F32 + ("info", "vert_off", "body_verts", "world_verts", "vert_owner", "xform"):
@@ -421,24 +434,32 @@ class Simulator:
     MUTABLE = ("pos", "dx_all", "vel", "vel_half", "w_half_bf", "w_bf", "w", "q", "q_half", "q_all", "q_acc")
 
     def host_state(self):
-        """Pinned host copies of the state the step updates (what a caller holding its state in host
-        memory, as the reference does, passes in and gets back)."""
-        return {k: self.t[k].cpu().pin_memory() for k in self.MUTABLE}
+        """Pinned host copy of the state the step updates (what a caller holding its state in host
+        memory, as the reference does, passes in and gets back): a dict of per-array views of one
+        pinned buffer (key "_buffer"), laid out as the device buffer."""
+        hb = self.mutable.cpu().pin_memory()
+        host = {"_buffer": hb}
+        off = 0
+        for k in self.MUTABLE:
+            v = self.t[k]
+            b = v.numel() * v.element_size()
+            host[k] = hb[off:off + b].view(v.dtype).view(v.shape)
+            off += b
+        return host
 
     def host_state_bytes(self):
-        return sum(self.t[k].numel() * self.t[k].element_size() for k in self.MUTABLE)
+        return int(self.mutable.numel())
 
     def step_host(self, host, n_steps=1, stream=None):
-        """Copy `host` (pinned) to the device, run n_steps, copy the state back into `host`.
-        Uses the captured graph when there is one (and n_steps is a multiple of its length)."""
-        for k in self.MUTABLE:
-            self.t[k].copy_(host[k], non_blocking=True)
+        """Copy `host` (pinned, from host_state) to the device, run n_steps, copy the state back into
+        `host`: one copy each way.  Uses the captured graph when there is one (and n_steps is a
+        multiple of its length)."""
+        self.mutable.copy_(host["_buffer"], non_blocking=True)
         if self.graph is not None and n_steps % self.graph_steps == 0:
             self.replay(n_steps // self.graph_steps)
         else:
             self.step(n_steps, stream)
-        for k in self.MUTABLE:
-            host[k].copy_(self.t[k], non_blocking=True)
+        host["_buffer"].copy_(self.mutable, non_blocking=True)
         return host
 
     # ------------------------------------------------------------------ inspection
