@@ -564,13 +564,43 @@ def batch_compare(args):
     e1.record(stream)
     torch.cuda.synchronize()
     ms_seq = e0.elapsed_time(e1) / K
+    stages = batch_stages(batch)
     return {"scenes": len(specs), "particles": int(n_total), "counts_min_max": [int(min(sp.n_particles for sp in specs)),
             int(max(sp.n_particles for sp in specs))], "build_s": build_s, "lanes_tuning_ms": tune,
             "lanes": batch.lanes, "ms_per_step_batched": ms_batch, "ms_per_step_sequential": ms_seq,
             "particle_steps_per_s_batched": n_total / (ms_batch * 1e-3),
             "particle_steps_per_s_sequential": n_total / (ms_seq * 1e-3),
             "batched_over_sequential": ms_seq / ms_batch, "identical_contact_sets": same,
-            "status": batch.status(), "pairs_batched": int(len(bp))}
+            "status": batch.status(), "pairs_batched": int(len(bp)), "stages": stages}
+
+
+def batch_stages(sim, reps=5):
+    """Per-stage device time of the batched step (CUDA events around each stage's launches; its
+    arrays, ~1.5 GB, are far larger than L2) and the HBM roofline of the integrator, the stage whose
+    traffic is fixed by the algorithm: per row 536 B (state read and written), per vertex 32 B (body
+    vertex in, world vertex out)."""
+    import torch
+    stream = torch.cuda.current_stream()
+    acc = {"broad": 0.0, "narrow": 0.0, "integrate": 0.0}
+    for _ in range(reps):
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        evs[0].record(stream)
+        sim.broadphase()
+        evs[1].record(stream)
+        sim.narrow_force()
+        evs[2].record(stream)
+        sim.integrate()
+        evs[3].record(stream)
+        torch.cuda.synchronize()
+        for k, (a, b) in zip(acc, ((0, 1), (1, 2), (2, 3))):
+            acc[k] += evs[a].elapsed_time(evs[b])
+    ms = {k: v / reps for k, v in acc.items()}
+    hbm = peaks().get("hbm_gbs", 6800.0)
+    ib = integrate_bytes(sim)
+    a = ib / (ms["integrate"] * 1e-3) / 1e9
+    return {"ms": ms, "integrate_roofline": {"kernel": "integrate_rows_kernel + world_verts_kernel", "bound": "hbm",
+                                            "bytes_per_step": ib, "achieved": a, "peak": hbm, "unit": "GB/s",
+                                            "frac": a / hbm}}
 
 
 def settling(args, steps=2000, cpu_seconds=20.0):
