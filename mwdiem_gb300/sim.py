@@ -299,7 +299,9 @@ class Simulator:
     def _build_work(self, pair_cap, collect_collisions):
         n = self.n
         n_part = sum(sp.n_particles for sp in self.specs)
-        cap = int(pair_cap) if pair_cap else max(4096, 16 * n_part)
+        # default capacity: the bounding-sphere filter keeps a few candidates per particle; the
+        # reference's full list (8-cell stencil, walls) holds up to ~30 per particle in dense packing
+        cap = int(pair_cap) if pair_cap else max(4096, (16 if self.cull_pairs else 40) * n_part)
         i32 = dict(dtype=torch.int32, device=self.device)
         w = {}
         w["cell_count"] = torch.zeros(max(self.total_cells, 1), **i32)
