@@ -517,6 +517,46 @@ class Simulator:
             out[r, :k] = wv[off[r]:off[r + 1], :3]
         return out
 
+    # ------------------------------------------------------------------ snapshots
+    SNAPSHOT = MUTABLE + ("world_verts", "force", "torque", "info")
+
+    def save(self, path):
+        """Write the simulated state to an .npz file: every array a step updates, the world vertices,
+        the force/torque accumulators, the row flags (an inlet activates rows), the inlet and
+        persistent-history tables when present, and the step count.  Call between steps."""
+        torch.cuda.synchronize()
+        out = {k: self.t[k].cpu().numpy() for k in self.SNAPSHOT}
+        out["steps_done"] = np.array(self.steps_done)
+        if self.inlet is not None:
+            for k in ("next_row", "step"):
+                out["inlet_" + k] = self.inlet_t[k].cpu().numpy()
+        if self.persistent_history:
+            for k in ("hist_keys", "hist_vals", "hist_parity"):
+                out[k] = self.w[k].cpu().numpy()
+        np.savez(path, **out)
+
+    def load(self, path):
+        """Restore a snapshot written by save() into this simulator, built from the same scenes with
+        the same options; a captured graph stays valid (the arrays are refilled in place)."""
+        z = np.load(path)
+        keys = list(self.SNAPSHOT)
+        if self.inlet is not None:
+            keys += ["inlet_next_row", "inlet_step"]
+        if self.persistent_history:
+            keys += ["hist_keys", "hist_vals", "hist_parity"]
+        for k in keys:
+            if k not in z.files:
+                raise ValueError(f"snapshot {path} has no {k!r}: written by a simulator with other options")
+            dst = (self.inlet_t[k[6:]] if k.startswith("inlet_") else
+                   self.w[k] if k.startswith("hist_") else self.t[k])
+            src = torch.from_numpy(z[k])
+            if tuple(src.shape) != tuple(dst.shape) or src.dtype != dst.dtype:
+                raise ValueError(f"snapshot array {k!r} is {tuple(src.shape)} {src.dtype}, this simulator's is "
+                                 f"{tuple(dst.shape)} {dst.dtype}")
+            dst.copy_(src)
+        self.steps_done = int(z["steps_done"])
+        self.w["status"].zero_()
+
     def reference_state(self):
         """State as the reference's FP64 arrays (MWDiem.py:603-631) plus per-row vertex counts."""
         t = {k: v.cpu().numpy() for k, v in self.t.items()}
