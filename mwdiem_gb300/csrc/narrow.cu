@@ -118,6 +118,43 @@ __device__ __forceinline__ void support(const Group<LPP>& g, const float4* hA, i
     s = mk3(a.x - b.x, a.y - b.y, a.z - b.z);
 }
 
+// The first two support queries of GJK, in directions d1 and d2 = -d1, in one pass over the hulls:
+// the same dot products, maxima and first-index ties as two calls of support() (the A side of d2
+// and the B side of d1 both use -d1 = d1 * -1, the B side of d2 uses d2 * -1 = d1), so the results
+// are those two calls'.  The second query's latency overlaps the first's; the caller counts it as
+// work only when GJK gets that far.
+template <int LPP>
+__device__ __forceinline__ void support_pair(const Group<LPP>& g, const float4* hA, int nA, const float4* hB, int nB,
+                                             f3 d1, f3& S1, int& a1, int& b1, f3& S2, int& a2, int& b2)
+{
+    const f3 n1 = d1 * (-1.f);
+    float tA = -1e30f, uA = -1e30f, tB = -1e30f, uB = -1e30f;
+    int itA = 0, iuA = 0, itB = 0, iuB = 0;
+#pragma unroll 4
+    for (int i = g.lane; i < nA; i += LPP) {
+        const float4 v = hA[i];
+        const float t = d1.x * v.x + d1.y * v.y + d1.z * v.z;
+        const float u = n1.x * v.x + n1.y * v.y + n1.z * v.z;
+        if (t > tA) { tA = t; itA = i; }
+        if (u > uA) { uA = u; iuA = i; }
+    }
+#pragma unroll 4
+    for (int j = g.lane; j < nB; j += LPP) {
+        const float4 v = hB[j];
+        const float t = d1.x * v.x + d1.y * v.y + d1.z * v.z;
+        const float u = n1.x * v.x + n1.y * v.y + n1.z * v.z;
+        if (t > tB) { tB = t; itB = j; }
+        if (u > uB) { uB = u; iuB = j; }
+    }
+    a1 = group_argmax<LPP>(g, tA, itA);  // support(d1): argmax d1.a, argmax (-d1).b
+    b1 = group_argmax<LPP>(g, uB, iuB);
+    a2 = group_argmax<LPP>(g, uA, iuA);  // support(d2): argmax (-d1).a, argmax d1.b
+    b2 = group_argmax<LPP>(g, tB, itB);
+    const float4 p1 = hA[a1], q1 = hB[b1], p2 = hA[a2], q2 = hB[b2];
+    S1 = mk3(p1.x - q1.x, p1.y - q1.y, p1.z - q1.z);
+    S2 = mk3(p2.x - q2.x, p2.y - q2.y, p2.z - q2.z);
+}
+
 // ---- simplex tests, identical on every lane (.cu:103-268) ----
 __device__ __forceinline__ void seg_test(f3 P1, f3 P2, int& coll, f3& d)
 {
@@ -794,10 +831,13 @@ __device__ int gjk_decide(const Group<LPP>& g, const float4* hA, int nA, const f
     f3 S1, S2, S3, S4, d3, d4;
     int a1, b1, a2, b2, a3, b3, a4 = 0, b4 = 0, todel = 0, coll = -1;
     f3 d1 = cB - cA;
-    support<LPP>(g, hA, nA, hB, nB, d1, S1, a1, b1, wk);
-    if (dot(d1, S1) < 0.f) return 0;
     f3 d2 = d1 * (-1.f);
-    support<LPP>(g, hA, nA, hB, nB, d2, S2, a2, b2, wk);
+    support_pair<LPP>(g, hA, nA, hB, nB, d1, S1, a1, b1, S2, a2, b2);
+    wk.dots += (uint32_t)(nA + nB);
+    wk.queries += 1;
+    if (dot(d1, S1) < 0.f) return 0;
+    wk.dots += (uint32_t)(nA + nB);
+    wk.queries += 1;
     if (dot(d2, S2) < 0.f) return 0;
     seg_test(S1, S2, coll, d3);
     if (coll == 0) return 0;
