@@ -126,23 +126,16 @@ __global__ void __launch_bounds__(SCAN_SMALL_THREADS) scan_small_kernel(const in
     }
 }
 
-// prefixed: block_sums already holds each tile's exclusive prefix (scanned by an earlier kernel);
-// otherwise every block adds up the totals of the tiles before it
 __global__ void scan_final_kernel(const int32_t* in, int64_t n, const int32_t* block_sums, int32_t* out, int nb,
-                                  int64_t* total_out, int64_t cap, uint32_t* status, uint32_t overflow_bit,
-                                  int prefixed)
+                                  int64_t* total_out, int64_t cap, uint32_t* status, uint32_t overflow_bit)
 {
     pdl_wait();
     pdl_launch_dependents();
     __shared__ int sh[SCAN_THREADS / 32];
+    int part = 0;
+    for (int i = threadIdx.x; i < (int)blockIdx.x; i += SCAN_THREADS) part += block_sums[i];
     int offset;
-    if (prefixed) {
-        offset = block_sums[blockIdx.x];
-    } else {
-        int part = 0;
-        for (int i = threadIdx.x; i < (int)blockIdx.x; i += SCAN_THREADS) part += block_sums[i];
-        block_exclusive_scan(part, sh, &offset);  // offset = sum over the whole block
-    }
+    block_exclusive_scan(part, sh, &offset);  // offset = sum over the whole block
     int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
     int v[SCAN_ITEMS];
     int s = 0;
@@ -730,7 +723,7 @@ int launch_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* tmp, int64_
     const int nbl = nb > 0 ? nb : 1;
     MWD_CUDA(launch_pdl(scan_reduce_kernel, nbl, SCAN_THREADS, 0, s, in, n, tmp));
     MWD_CUDA(launch_pdl(scan_final_kernel, nbl, SCAN_THREADS, 0, s, in, n, tmp, out, nbl, total_out, cap, status,
-                        overflow_bit, 0));
+                        overflow_bit));
     MWD_CUDA(cudaGetLastError());
     return MWD_OK;
 }
@@ -752,7 +745,7 @@ int launch_broad(const BroadArgs& a, cudaStream_t s)
         const int nb = (int)((a.total_cells + SCAN_TILE - 1) / SCAN_TILE);
         MWD_CUDA(launch_pdl(scan_final_kernel, nb, SCAN_THREADS, 0, s, (const int32_t*)a.cell_count, a.total_cells,
                             (const int32_t*)a.tile_sums, a.cell_start, nb, (int64_t*)nullptr, (int64_t)INT64_MAX,
-                            (uint32_t*)nullptr, 0u, 0));
+                            (uint32_t*)nullptr, 0u));
     } else {
         rc = launch_scan(a.cell_count, a.total_cells, a.cell_start, a.scan_tmp, nullptr, INT64_MAX, nullptr, 0, s);
         if (rc) return rc;
