@@ -85,7 +85,7 @@ def parse():
     ap.add_argument("--calibration", action="store_true",
                     help="differentiable calibration: 2,000 hulls, 5,000 steps, forward vs forward + adjoint")
     ap.add_argument("--settling", action="store_true",
-                    help="config 1 (125 cubes, dt 1e-4, 2000 steps): the reference CPU path (oracle "
+                    help="the 125-cube settling scene (dt 1e-4, 2000 steps): the reference CPU path (oracle "
                          "restatement, one core) and the device step")
     ap.add_argument("--calib-steps", type=int, default=5000)
     ap.add_argument("--calib-particles", type=int, default=2000)
@@ -93,7 +93,7 @@ def parse():
                     help="calibration's torque-arm contact point: the reference's (cpA - cpB)/2 spins particles "
                          "far from the origin up until the 5,000-step pour flies apart, so the midpoint is the default")
     ap.add_argument("--batch-only", action="store_true",
-                    help="only the batched step (config 4) with --lanes (no tuning, no sequential comparison)")
+                    help="only the 256-scene batched step with --lanes (no tuning, no sequential comparison)")
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--batch-total", type=int, default=2_000_000)
     return ap.parse_args()
@@ -523,7 +523,7 @@ def pairs_rate(n_pairs, lanes, reps=5, with_cpu=True, fixed=None):
 
 
 def batch_compare(args):
-    """Config 4: independent boxes with log-uniform particle counts (cubes, tetrahedra, hulls), dt 5e-5.
+    """256 independent boxes with log-uniform particle counts (cubes, tetrahedra, hulls), dt 5e-5.
     Batched = all scenes in one state, one launch per stage, one CUDA graph per step, lanes chosen by
     the autotuner.  Sequential = one simulator per scene, stepped one after another with plain
     launches.  Contact sets are compared scene by scene after the first broad phase."""
@@ -604,7 +604,7 @@ def batch_stages(sim, reps=5):
 
 
 def settling(args, steps=2000, cpu_seconds=20.0):
-    """Config 1: 125 randomly rotated unit cubes on a 5^3 lattice (spacing 1.5) settling onto a floor,
+    """The settling scene: 125 randomly rotated unit cubes on a 5^3 lattice (spacing 1.5) onto a floor,
     dt 1e-4, 2000 steps.  The reference CPU path (wall test + Linked_cell_hash + per-pair gather +
     contact kernel FP32 + Verlet kernel FP64, as the oracle restates them) is timed on one host core
     for the whole run or ~20 s, whichever ends first; the device step (graph replay) runs all 2000
@@ -650,7 +650,7 @@ def settling(args, steps=2000, cpu_seconds=20.0):
 
 
 def batch_only(args):
-    """Config 4's batched step alone: all scenes in one state, the step captured in one CUDA graph,
+    """The 256-scene batched step alone: all scenes in one state, the step captured in one CUDA graph,
     --lanes fixed, --warmup then --steps replays timed with CUDA events."""
     import torch
     from mwdiem_gb300 import scene
@@ -673,7 +673,7 @@ def batch_only(args):
 
 
 def calibration(args):
-    """Config 5: 2,000 random hulls (12-32 points, radius U[0.8,1.2]) poured in a 20 x 20 box, 5,000
+    """Calibration: 2,000 random hulls (12-32 points, radius U[0.8,1.2]) poured in a 20 x 20 box, 5,000
     steps at dt 5e-5.  Loss = MSE of the per-step centre of mass against a target trajectory of the
     same simulator with kn 2e5, damping ratio 0.2, mu 0.4; gradients with respect to kn, damping
     ratio, mu and the initial velocities, checkpoints every 100 steps.  Times the differentiable

@@ -18,9 +18,9 @@ Variants (``variant=``):
   ``"histfix"``  FP32 contact kernel with the tangential-history index ``displacement_tang[P+k]``
                  turned into ``displacement_tang[4*P+k]`` (the stride the arrays are allocated with).
 
-The reference source is read from ``/root/reference`` when it exists (this build container).  The
-rendered ``.cpp`` files are kept next to the ``.so`` so that a machine without the reference (the
-GPU machine) can still compile the same renderings: ``ensure_built`` falls back to compiling an existing
+The reference source is read from ``/root/reference`` when it exists.  The rendered ``.cpp`` files
+are kept next to the ``.so`` so that a machine without the reference checkout can still compile the
+same renderings: ``ensure_built`` falls back to compiling an existing
 rendered file.  Compiled with ``-ffp-contract=off`` because GCC on aarch64 fuses multiply-adds by
 default, which would change FP32 rounding relative to the CUDA build (``--fmad=false``).
 """

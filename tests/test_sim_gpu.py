@@ -281,7 +281,7 @@ def test_deterministic_mode_is_reproducible():
 
 
 def test_settling_config1_short_horizon():
-    # config 1 (125 unit cubes on a 5^3 lattice at spacing 1.5, random orientations, onto a floor,
+    # the settling scene (125 unit cubes on a 5^3 lattice at spacing 1.5, random orientations, onto a floor,
     # dt 1e-4): rotated cubes reach 0.87 from their centres, so neighbours overlap from step 0 and the
     # reference path's motion turns violent within the first hundred steps; the FP32 device step is
     # compared with the FP64 reference path over the first 20 steps
@@ -302,7 +302,7 @@ def test_settling_config1_short_horizon():
     vmax = np.abs(ref.st["v"][W:]).max()
     dvel = np.abs(g["v"][W:] - ref.st["v"][W:]).max()
     dq = np.abs(g["q"][W:] - ref.st["q"][W:]).max()
-    print(f"config 1, {steps} steps: |dpos| {dpos:.3e} |dv| {dvel:.3e} (vmax {vmax:.3e}) |dq| {dq:.3e}")
+    print(f"settling scene, {steps} steps: |dpos| {dpos:.3e} |dv| {dvel:.3e} (vmax {vmax:.3e}) |dq| {dq:.3e}")
     assert dpos <= 2e-6 * size
     assert dvel <= 1e-3 * vmax
     assert dq <= 1e-4
