@@ -297,15 +297,10 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     clk = clocks.stop()
-    total_ms = sum(a.elapsed_time(b) for a, b in ev)
-    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t.item())
+    value, total_ms = job_rate(sum(a.elapsed_time(b) for a, b in ev), N_PARTICLES * args.steps, world, "cuda")
     status = sim.check_status()
     n_pairs = sim.n_pairs()
     nonfinite = sim.nonfinite_rows()
-    value = N_PARTICLES * args.steps * world / (total_ms * 1e-3)
 
     # e2e: state from pinned host memory in, result back out, every step (from the initial state)
     window.restore()
@@ -320,12 +315,8 @@ def main():
         sim.step_host(host, 1)
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1)
-    te = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e = {"value": N_PARTICLES * ne * world / (float(te.item()) * 1e-3), "unit": METRIC,
-           "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+    e2e_value, _ = job_rate(e0.elapsed_time(e1), N_PARTICLES * ne, world, "cuda")
+    e2e = {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
 
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -358,6 +349,18 @@ def main():
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def job_rate(local_ms, units_per_rank, world, device):
+    """Whole-job throughput of `world` independent replicas (one per GPU, the same work each): the
+    units all ranks processed over the slowest rank's time (max over ranks).  Returns (units/s, ms)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    return units_per_rank * world / (ms * 1e-3), ms
 
 
 def breakdown(sim, V, flush, reps=10):
