@@ -342,6 +342,10 @@ int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work*
  * rewrites world_verts, zeroes force/torque. */
 int mwd_integrate(mwd_state* st, const mwd_scene* scenes_dev, uint32_t* status, mwd_stream_t stream);
 
+/* World vertices (and the row transforms in st->xform) from the current centres and orientations:
+ * world = pos + R(q_acc) r0 for every row.  Needs vert_owner and xform. */
+int mwd_refresh_vertices(mwd_state* st, mwd_stream_t stream);
+
 /* broad phase + narrow phase + integrator, n_steps times. */
 int mwd_step(mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes_host, int32_t n_scenes,
              mwd_work* work, int32_t lanes, int32_t n_steps, mwd_stream_t stream);

@@ -508,6 +508,15 @@ int mwd_integrate(mwd_state* st, const mwd_scene* scenes_dev, uint32_t* status, 
     return launch_integrate(*st, scenes_dev, status, reinterpret_cast<cudaStream_t>(stream));
 }
 
+int mwd_refresh_vertices(mwd_state* st, mwd_stream_t stream)
+{
+    if (!st || !st->vert_owner || !st->xform) {
+        set_error("mwd_refresh_vertices: needs a state with vert_owner and xform");
+        return MWD_ERR_INVALID;
+    }
+    return launch_refresh_vertices(*st, reinterpret_cast<cudaStream_t>(stream));
+}
+
 int mwd_step(mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes_host, int32_t n_scenes, mwd_work* work,
              int32_t lanes, int32_t n_steps, mwd_stream_t stream)
 {

@@ -388,6 +388,24 @@ __global__ void __launch_bounds__(RB) integrate_rows_kernel(mwd_state st, const 
     o[3] = make_float4(x[12], x[13], x[14], x[15]);
 }
 
+// the row transforms alone, from the current centres and orientations (no integration)
+__global__ void __launch_bounds__(RB) xform_rows_kernel(mwd_state st)
+{
+    pdl_wait();
+    pdl_launch_dependents();
+    const int P = blockIdx.x * RB + threadIdx.x;
+    if (P >= st.n) return;
+    const dpos pos = reinterpret_cast<const dpos*>(st.pos)[P];
+    float x[16];
+    row_xform(ld4(st.q_acc, P), pos, x, x + 9);
+    x[15] = 0.f;
+    float4* o = reinterpret_cast<float4*>(st.xform) + 4 * (size_t)P;
+    o[0] = make_float4(x[0], x[1], x[2], x[3]);
+    o[1] = make_float4(x[4], x[5], x[6], x[7]);
+    o[2] = make_float4(x[8], x[9], x[10], x[11]);
+    o[3] = make_float4(x[12], x[13], x[14], x[15]);
+}
+
 // the vertex pass of the split integrator: one thread per vertex
 __global__ void __launch_bounds__(256) world_verts_kernel(mwd_state st)
 {
@@ -418,6 +436,13 @@ int launch_world_verts(const mwd_state& st, cudaStream_t s)
     if (st.n_verts <= 0) return MWD_OK;
     MWD_CUDA(launch_pdl(world_verts_kernel, (st.n_verts + 255) / 256, 256, 0, s, st));
     return MWD_OK;
+}
+
+int launch_refresh_vertices(const mwd_state& st, cudaStream_t s)
+{
+    if (st.n <= 0) return MWD_OK;
+    MWD_CUDA(launch_pdl(xform_rows_kernel, (st.n + RB - 1) / RB, RB, 0, s, st));
+    return launch_world_verts(st, s);
 }
 
 int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, cudaStream_t s)

@@ -20,5 +20,7 @@ int launch_verlet_ref(const VerletRefArgs& a, cudaStream_t s);
 int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, cudaStream_t s);
 // world vertices from st.xform (row transforms) through st.vert_owner, one thread per vertex
 int launch_world_verts(const mwd_state& st, cudaStream_t s);
+// row transforms + world vertices from the current state (no integration)
+int launch_refresh_vertices(const mwd_state& st, cudaStream_t s);
 
 }  // namespace mwd

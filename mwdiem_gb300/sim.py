@@ -218,18 +218,8 @@ class Simulator:
         t["vert_off"] = off_d.to(torch.int32)
         t["body_verts"] = body
         owner = torch.repeat_interleave(torch.arange(n, device=dev), counts_d)
+        # world vertices: written below by the device's own transform (as every step writes them)
         world = body.clone()
-        world[:, :3] = (t["pos"][owner, :3] + body[:, :3].double()).float()
-        turned = torch.from_numpy(np.nonzero(np.any(cat["q0"] != [1.0, 0.0, 0.0, 0.0], axis=1))[0]).to(dev)
-        if len(turned):  # principal-axes rows start at q0: world = pos + R(q0) r_p
-            sel = torch.isin(owner, turned).nonzero().squeeze(1)
-            q0d = torch.from_numpy(cat["q0"]).to(dev)
-            chunk = 1 << 20
-            for a0 in range(0, len(sel), chunk):
-                vi = sel[a0:a0 + chunk]
-                R = _quat_to_matrix(q0d[owner[vi]])
-                rot = torch.einsum("vij,vj->vi", R, body[vi, :3].double())
-                world[vi, :3] = (t["pos"][owner[vi], :3] + rot).float()
         t["world_verts"] = world
         # the integrator's vertex pass: one thread per vertex, through each row's transform
         t["vert_owner"] = owner.to(torch.int32)
@@ -255,6 +245,10 @@ class Simulator:
         st.n_verts = total
         st.max_verts = self.max_verts
         self.state = st
+        # world = pos + R(q_acc) r0 with the integrator's arithmetic, so that the first step sees the
+        # vertices every later step sees (q_acc is the principal-frame orientation q0 under the
+        # physical law, identity otherwise)
+        check(lib().mwd_refresh_vertices(C.byref(st), _dev.stream_handle()))
 
     def _build_scenes(self):
         S = len(self.specs)
