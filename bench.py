@@ -94,6 +94,7 @@ def parse():
                          "far from the origin up until the 5,000-step pour flies apart, so the midpoint is the default")
     ap.add_argument("--batch-only", action="store_true",
                     help="only the 256-scene batched step with --lanes (no tuning, no sequential comparison)")
+    ap.add_argument("--graph-steps", type=int, default=1, help="steps per captured graph (--batch-only)")
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--batch-total", type=int, default=2_000_000)
     return ap.parse_args()
@@ -553,7 +554,10 @@ def batch_compare(args):
             same = False
     tune = autotune.tune_lanes(batch, steps=3)
     K = max(1, args.steps)
-    ms_batch = autotune.time_steps(batch, steps=K, reps=3)
+    # one step per graph, then ten: inside a ten-step graph each step's world-vertex pass runs beside
+    # the next step's broad phase (mwd_step's overlap); the arrays (~1.5 GB) are far larger than L2
+    ms_batch_1 = autotune.time_steps(batch, steps=K, reps=3)
+    ms_batch = autotune.time_steps(batch, steps=max(K, 10), reps=3, per=10)
     stream = torch.cuda.current_stream()
     for one in singles:
         one.lanes = batch.lanes
@@ -570,7 +574,8 @@ def batch_compare(args):
     stages = batch_stages(batch)
     return {"scenes": len(specs), "particles": int(n_total), "counts_min_max": [int(min(sp.n_particles for sp in specs)),
             int(max(sp.n_particles for sp in specs))], "build_s": build_s, "lanes_tuning_ms": tune,
-            "lanes": batch.lanes, "ms_per_step_batched": ms_batch, "ms_per_step_sequential": ms_seq,
+            "lanes": batch.lanes, "ms_per_step_batched": ms_batch, "graph_steps_batched": 10,
+            "ms_per_step_batched_graph1": ms_batch_1, "ms_per_step_sequential": ms_seq,
             "particle_steps_per_s_batched": n_total / (ms_batch * 1e-3),
             "particle_steps_per_s_sequential": n_total / (ms_seq * 1e-3),
             "batched_over_sequential": ms_seq / ms_batch, "identical_contact_sets": same,
@@ -661,17 +666,19 @@ def batch_only(args):
     specs = scene.batched_scenes(n_scenes=args.batch_scenes, total=args.batch_total, seed=0)
     n_total = sum(sp.n_particles for sp in specs)
     sim = Simulator(specs, lanes=args.lanes)
-    sim.capture(1)
-    sim.replay(max(1, args.warmup))
+    per = max(1, args.graph_steps)
+    n = max(1, -(-max(1, args.steps) // per))
+    sim.capture(per)
+    sim.replay(max(1, -(-args.warmup // per)))
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    sim.replay(max(1, args.steps))
+    sim.replay(n)
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / max(1, args.steps)
-    return {"scenes": len(specs), "particles": int(n_total), "lanes": args.lanes, "ms_per_step": ms,
+    ms = e0.elapsed_time(e1) / (n * per)
+    return {"scenes": len(specs), "particles": int(n_total), "lanes": args.lanes, "graph_steps": per, "ms_per_step": ms,
             "particle_steps_per_s": n_total / (ms * 1e-3), "status": sim.status()}
 
 

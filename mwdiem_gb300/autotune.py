@@ -14,18 +14,20 @@ import copy
 import torch
 
 
-def time_steps(sim, steps=5, reps=3):
-    """Median ms per graph-replayed step (after one captured warm-up step)."""
-    sim.capture(1)
+def time_steps(sim, steps=5, reps=3, per=1):
+    """Median ms per graph-replayed step (after one captured warm-up step); `per` steps per graph
+    (rounded up to whole graphs)."""
+    sim.capture(per)
+    n = max(1, -(-steps // per))
     stream = torch.cuda.current_stream()
     best = []
     for _ in range(reps):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        sim.replay(steps)
+        sim.replay(n)
         e1.record(stream)
         torch.cuda.synchronize()
-        best.append(e0.elapsed_time(e1) / steps)
+        best.append(e0.elapsed_time(e1) / (n * per))
     best.sort()
     return best[len(best) // 2]
 

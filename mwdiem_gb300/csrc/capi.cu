@@ -131,6 +131,62 @@ static void derive_one(double Kn, double en, double et, double mu, double dt, in
 
 }  // namespace mwd
 
+thread_local int mwd::g_launch_priority = 0;
+
+namespace {
+
+// The second stream and the two events of the overlapped multi-step mwd_step, one set per device.
+// They are created outside any stream capture: by the first mwd_step call that could overlap (a
+// one-step call included, such as the warm-up step before a graph capture); a call that finds none
+// while its stream is being captured steps without the overlap.
+struct SideStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    int prio_high = 0;
+};
+std::mutex g_side_mu;
+SideStream g_side[64];
+
+const SideStream* side_stream(cudaStream_t main)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_side_mu);
+    SideStream& ss = g_side[dev];
+    if (ss.s) return &ss;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(main, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return nullptr;
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return nullptr;
+    cudaStream_t st = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, least) != cudaSuccess) return nullptr;
+    if (cudaEventCreateWithFlags(&a, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b, cudaEventDisableTiming) != cudaSuccess) {
+        if (a) cudaEventDestroy(a);
+        cudaStreamDestroy(st);
+        return nullptr;
+    }
+    ss.fork = a;
+    ss.join = b;
+    ss.prio_high = greatest;
+    ss.s = st;
+    return &ss;
+}
+
+// MWD_OVERLAP=0 in the environment: multi-step calls run the plain loop
+bool overlap_enabled()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("MWD_OVERLAP");
+        v = (e && e[0] == '0') ? 0 : 1;
+    }
+    return v == 1;
+}
+
+}  // namespace
+
 bool mwd::pdl_enabled()
 {
     static int v = -1;
@@ -520,17 +576,41 @@ int mwd_refresh_vertices(mwd_state* st, mwd_stream_t stream)
 int mwd_step(mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes_host, int32_t n_scenes, mwd_work* work,
              int32_t lanes, int32_t n_steps, mwd_stream_t stream)
 {
+    // Several steps in one call: the world-vertex pass of step i-1 runs on a second stream beside the
+    // broad phase of step i (which reads centres and radii, not vertices), whose kernels get the
+    // higher launch priority, and is joined before the narrow phase; the last step's pass runs in
+    // line, so the state is complete when the call's work ends.  Every kernel computes what it
+    // computes in the plain loop, so the results are the same.
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const SideStream* side = nullptr;
+    if (!work->inlet && st->vert_owner && st->xform && st->n > 0 && st->n_verts > 0 && overlap_enabled())
+        side = side_stream(s);
+    const bool ovl = side && n_steps > 1;
     for (int i = 0; i < n_steps; ++i) {
         if (work->inlet) {
             int rc0 = mwd_inlet_step(st, work->inlet, stream);
             if (rc0) return rc0;
         }
-        int rc = mwd_broadphase(st, scenes_dev, scenes_host, n_scenes, work, stream);
+        const bool fork = ovl && i > 0;
+        if (fork) {
+            MWD_CUDA(cudaEventRecord(side->fork, s));
+            MWD_CUDA(cudaStreamWaitEvent(side->s, side->fork, 0));
+            int rcv = launch_world_verts(*st, side->s);
+            if (rcv) return rcv;
+            MWD_CUDA(cudaEventRecord(side->join, side->s));
+        }
+        int rc;
+        {
+            LaunchPriority lp(fork ? side->prio_high : 0);
+            rc = mwd_broadphase(st, scenes_dev, scenes_host, n_scenes, work, stream);
+        }
         if (rc) return rc;
+        if (fork) MWD_CUDA(cudaStreamWaitEvent(s, side->join, 0));
         // the broad phase zeroed the EPA counter (assign_kernel): no memset node between the kernels
         rc = narrow_force(st, scenes_dev, work, lanes, stream, true);
         if (rc) return rc;
-        rc = mwd_integrate(st, scenes_dev, work->status, stream);
+        rc = (ovl && i < n_steps - 1) ? launch_integrate(*st, scenes_dev, work->status, s, false)
+                                      : mwd_integrate(st, scenes_dev, work->status, stream);
         if (rc) return rc;
     }
     return MWD_OK;

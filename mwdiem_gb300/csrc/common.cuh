@@ -103,6 +103,16 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
 __device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 bool pdl_enabled();
 
+// Priority given to the kernels launch_pdl launches from this thread (0: the stream's own).  A
+// multi-step mwd_step raises it for the broad phase while the previous step's world-vertex pass runs
+// beside it on a second stream, so that the broad phase's blocks take the SMs first.
+extern thread_local int g_launch_priority;
+struct LaunchPriority {
+    int saved;
+    explicit LaunchPriority(int p) : saved(g_launch_priority) { g_launch_priority = p; }
+    ~LaunchPriority() { g_launch_priority = saved; }
+};
+
 // offsets of 256-byte aligned sub-arrays in one scratch allocation
 struct Carver {
     size_t off = 0;
@@ -123,11 +133,20 @@ cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
     cfg.blockDim = block;
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchAttribute at[2];
+    unsigned na = 0;
+    if (pdl_enabled()) {
+        at[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[na].val.programmaticStreamSerializationAllowed = 1;
+        ++na;
+    }
+    if (g_launch_priority) {
+        at[na].id = cudaLaunchAttributePriority;
+        at[na].val.priority = g_launch_priority;
+        ++na;
+    }
     cfg.attrs = at;
-    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    cfg.numAttrs = na;
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 }  // namespace mwd

@@ -445,12 +445,14 @@ int launch_refresh_vertices(const mwd_state& st, cudaStream_t s)
     return launch_world_verts(st, s);
 }
 
-int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, cudaStream_t s)
+int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, cudaStream_t s,
+                     bool with_verts)
 {
     if (st.n <= 0) return MWD_OK;
     if (st.vert_owner && st.xform) {
         MWD_CUDA(launch_pdl(integrate_rows_kernel, (st.n + RB - 1) / RB, RB, 0, s, st, scenes, status));
-        if (st.n_verts > 0) MWD_CUDA(launch_pdl(world_verts_kernel, (st.n_verts + 255) / 256, 256, 0, s, st));
+        if (with_verts && st.n_verts > 0)
+            MWD_CUDA(launch_pdl(world_verts_kernel, (st.n_verts + 255) / 256, 256, 0, s, st));
     } else {
         MWD_CUDA(launch_pdl(integrate_kernel, (st.n + RB - 1) / RB, RB, 0, s, st, scenes, status));
     }

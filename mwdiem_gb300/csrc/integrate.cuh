@@ -17,7 +17,10 @@ struct VerletRefArgs {
 };
 
 int launch_verlet_ref(const VerletRefArgs& a, cudaStream_t s);
-int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, cudaStream_t s);
+// with_verts false (only with st.vert_owner and st.xform): the row pass alone; the world vertices are
+// then rewritten from st.xform by a later launch_world_verts
+int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, cudaStream_t s,
+                     bool with_verts = true);
 // world vertices from st.xform (row transforms) through st.vert_owner, one thread per vertex
 int launch_world_verts(const mwd_state& st, cudaStream_t s);
 // row transforms + world vertices from the current state (no integration)
