@@ -303,10 +303,13 @@ def main():
     n_pairs = sim.n_pairs()
     nonfinite = sim.nonfinite_rows()
 
-    # e2e: state from pinned host memory in, result back out, every step (from the initial state)
+    # e2e: state from pinned host memory in, result back out, every step (from the initial state), one
+    # captured graph per step: centres in, broad phase while the rest of the state comes in, narrow
+    # phase, integrator, state out (Simulator.capture_host)
     window.restore()
     host = sim.host_state()
     nbytes = sim.host_state_bytes()
+    sim.capture_host(host)
     sim.step_host(host, 1)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -342,6 +342,12 @@ int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work*
  * rewrites world_verts, zeroes force/torque. */
 int mwd_integrate(mwd_state* st, const mwd_scene* scenes_dev, uint32_t* status, mwd_stream_t stream);
 
+/* mwd_integrate in two parts (a state with vert_owner and xform): the row pass (state, forces zeroed,
+ * each row's transform into st->xform), then the vertex pass (world_verts from st->xform).  Between
+ * the two the state is final, so a copy of it may run beside the vertex pass. */
+int mwd_integrate_rows(mwd_state* st, const mwd_scene* scenes_dev, uint32_t* status, mwd_stream_t stream);
+int mwd_world_vertices(mwd_state* st, mwd_stream_t stream);
+
 /* World vertices (and the row transforms in st->xform) from the current centres and orientations:
  * world = pos + R(q_acc) r0 for every row.  Needs vert_owner and xform. */
 int mwd_refresh_vertices(mwd_state* st, mwd_stream_t stream);

@@ -564,6 +564,24 @@ int mwd_integrate(mwd_state* st, const mwd_scene* scenes_dev, uint32_t* status, 
     return launch_integrate(*st, scenes_dev, status, reinterpret_cast<cudaStream_t>(stream));
 }
 
+int mwd_integrate_rows(mwd_state* st, const mwd_scene* scenes_dev, uint32_t* status, mwd_stream_t stream)
+{
+    if (!st || !scenes_dev || !st->vert_owner || !st->xform) {
+        set_error("mwd_integrate_rows: needs scenes and a state with vert_owner and xform");
+        return MWD_ERR_INVALID;
+    }
+    return launch_integrate(*st, scenes_dev, status, reinterpret_cast<cudaStream_t>(stream), false);
+}
+
+int mwd_world_vertices(mwd_state* st, mwd_stream_t stream)
+{
+    if (!st || !st->vert_owner || !st->xform) {
+        set_error("mwd_world_vertices: needs a state with vert_owner and xform");
+        return MWD_ERR_INVALID;
+    }
+    return launch_world_verts(*st, reinterpret_cast<cudaStream_t>(stream));
+}
+
 int mwd_refresh_vertices(mwd_state* st, mwd_stream_t stream)
 {
     if (!st || !st->vert_owner || !st->xform) {

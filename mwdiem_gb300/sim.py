@@ -73,6 +73,8 @@ class Simulator:
             self._build_inlet(inlet)
         self.graph = None
         self.graph_steps = 0
+        self.host_graph = None
+        self.host_graph_buffer = None
         self.steps_done = 0
 
     # ------------------------------------------------------------------ set-up
@@ -408,6 +410,15 @@ class Simulator:
         check(lib().mwd_integrate(C.byref(self.state), self.scenes_dev.data_ptr(), self.w["status"].data_ptr(),
                                   _dev.stream_handle(stream)))
 
+    def integrate_rows(self, stream=None):
+        """The integrator's row pass alone (the state is final after it; world vertices follow from
+        world_vertices())."""
+        check(lib().mwd_integrate_rows(C.byref(self.state), self.scenes_dev.data_ptr(), self.w["status"].data_ptr(),
+                                       _dev.stream_handle(stream)))
+
+    def world_vertices(self, stream=None):
+        check(lib().mwd_world_vertices(C.byref(self.state), _dev.stream_handle(stream)))
+
     def capture(self, steps_per_replay=1):
         """Capture `steps_per_replay` steps in one CUDA graph (warm-up step first, outside capture)."""
         self.step(1)
@@ -448,8 +459,12 @@ class Simulator:
 
     def step_host(self, host, n_steps=1, stream=None):
         """Copy `host` (pinned, from host_state) to the device, run n_steps, copy the state back into
-        `host`: one copy each way.  Uses the captured graph when there is one (and n_steps is a
-        multiple of its length)."""
+        `host`: one copy each way.  One step on the `host` given to capture_host replays that graph;
+        otherwise the step graph is used when there is one (and n_steps is a multiple of its length)."""
+        if n_steps == 1 and self.host_graph is not None and host["_buffer"] is self.host_graph_buffer:
+            self.host_graph.replay()
+            self.steps_done += 1
+            return host
         self.mutable.copy_(host["_buffer"], non_blocking=True)
         if self.graph is not None and n_steps % self.graph_steps == 0:
             self.replay(n_steps // self.graph_steps)
@@ -457,6 +472,40 @@ class Simulator:
             self.step(n_steps, stream)
         host["_buffer"].copy_(self.mutable, non_blocking=True)
         return host
+
+    def capture_host(self, host):
+        """Capture one step between the pinned buffers of `host` (from host_state) in one CUDA graph,
+        replayed by step_host(host, 1).  The centres, the first array of the state, are copied in
+        first and the broad phase (which reads no other array of the state) starts on them while the
+        rest of the state is copied in on a second stream; the narrow phase waits for that copy.  The
+        state goes back to `host` after the integrator's row pass, beside its vertex pass.  The same
+        kernels as step(): the same results.  Not with an inlet (its rows enter inside mwd_step)."""
+        if self.inlet is not None:
+            raise ValueError("capture_host: the inlet runs inside mwd_step; use step_host without capture")
+        hb = host["_buffer"]
+        self.step_host(host, 1)  # warm-up outside capture
+        torch.cuda.synchronize()
+        npos = self.t["pos"].numel() * self.t["pos"].element_size()
+        side = torch.cuda.Stream(device=self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            main = torch.cuda.current_stream()
+            self.mutable[:npos].copy_(hb[:npos], non_blocking=True)
+            side.wait_stream(main)  # after the centres: one copy engine would otherwise take them second
+            with torch.cuda.stream(side):
+                self.mutable[npos:].copy_(hb[npos:], non_blocking=True)
+            self.broadphase()
+            main.wait_stream(side)
+            self.narrow_force()
+            self.integrate_rows()
+            side.wait_stream(main)
+            with torch.cuda.stream(side):
+                hb.copy_(self.mutable, non_blocking=True)
+            self.world_vertices()
+            main.wait_stream(side)
+        self.host_graph = g
+        self.host_graph_buffer = hb
+        return g
 
     # ------------------------------------------------------------------ inspection
     def status(self) -> int:

@@ -104,6 +104,24 @@ def test_host_round_trip_matches_device_stepping():
         assert torch.equal(host[k], b.t[k].cpu()), k
 
 
+def test_host_graph_matches_device_stepping():
+    # the captured host step (centres copied in first, the broad phase overlapping the copy of the
+    # rest of the state) gives the state of plain device steps, bit for bit (deterministic sums)
+    from mwdiem_gb300.sim import Simulator
+    sp = dense_scene(n=300, seed=8, spacing=2.3, vel=0.2)
+    a = Simulator(sp, deterministic=True)
+    b = Simulator(sp, deterministic=True)
+    host = a.host_state()
+    a.capture_host(host)         # one warm-up step through the plain host path
+    for _ in range(6):
+        a.step_host(host, 1)     # graph replays
+    b.step(7)
+    torch.cuda.synchronize()
+    assert a.steps_done == 7
+    for k in a.MUTABLE:
+        assert torch.equal(host[k], b.t[k].cpu()), k
+
+
 def test_snapshot_resume_continues_identically(tmp_path):
     # save after 5 steps, load into a fresh simulator of the same scene, 5 more steps on both:
     # identical states (deterministic sums), persistent history included
