@@ -354,8 +354,9 @@ int mwd_refresh_vertices(mwd_state* st, mwd_stream_t stream);
 
 /* broad phase + narrow phase + integrator, n_steps times.  With n_steps > 1 (and a state with
  * vert_owner and xform, no inlet) the world-vertex pass of each step but the last runs during the
- * next step's broad phase, on a second stream of the library's that is joined before the narrow
- * phase: the same results, and the state is complete when the call's work on `stream` ends.
+ * next step's broad phase, on a second stream of the library's (one per device and calling thread)
+ * that is joined before the narrow phase: the same results, and the state is complete when the
+ * call's work on `stream` ends.
  * MWD_OVERLAP=0 in the environment turns this off. */
 int mwd_step(mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes_host, int32_t n_scenes,
              mwd_work* work, int32_t lanes, int32_t n_steps, mwd_stream_t stream);

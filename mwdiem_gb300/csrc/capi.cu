@@ -135,8 +135,9 @@ thread_local int mwd::g_launch_priority = 0;
 
 namespace {
 
-// The second stream and the two events of the overlapped multi-step mwd_step, one set per device.
-// They are created outside any stream capture: by the first mwd_step call that could overlap (a
+// The second stream and the two events of the overlapped multi-step mwd_step, one set per device and
+// calling thread (so that calls from several threads never re-record each other's events).  They are
+// created outside any stream capture: by the thread's first mwd_step call that could overlap (a
 // one-step call included, such as the warm-up step before a graph capture); a call that finds none
 // while its stream is being captured steps without the overlap.
 struct SideStream {
@@ -144,14 +145,12 @@ struct SideStream {
     cudaEvent_t fork = nullptr, join = nullptr;
     int prio_high = 0;
 };
-std::mutex g_side_mu;
-SideStream g_side[64];
+thread_local SideStream g_side[64];
 
 const SideStream* side_stream(cudaStream_t main)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-    std::lock_guard<std::mutex> lk(g_side_mu);
     SideStream& ss = g_side[dev];
     if (ss.s) return &ss;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
