@@ -183,6 +183,41 @@ def test_multi_step_overlap_is_exact():
             assert np.array_equal(ta, o.t[k].cpu().numpy(), equal_nan=True), k
 
 
+def test_multi_step_calls_from_two_threads():
+    # two host threads, each stepping its own simulator ten steps per call on its own stream (each
+    # thread has its own overlap stream and events): the bits of the same calls made one after another
+    import threading
+    from mwdiem_gb300.sim import Simulator
+    specs = [dense_scene(n=500, seed=31), dense_scene(n=700, seed=32)]
+    ref = [Simulator(sp, deterministic=True) for sp in specs]
+    for r in ref:
+        r.step(10)
+    torch.cuda.synchronize()
+    sims = [Simulator(sp, deterministic=True) for sp in specs]
+    torch.cuda.synchronize()  # their set-up ran on the default stream
+    errors = []
+
+    def run(sim):
+        try:
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                sim.step(10)
+            s.synchronize()
+        except Exception as e:  # reported by the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(sim,)) for sim in sims]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    torch.cuda.synchronize()
+    assert not errors, errors
+    for r, sim in zip(ref, sims):
+        for k in ("pos", "q", "vel", "world_verts"):
+            assert np.array_equal(r.t[k].cpu().numpy(), sim.t[k].cpu().numpy(), equal_nan=True), k
+
+
 def test_batched_equals_separate():
     from mwdiem_gb300.sim import Simulator
     specs = [dense_scene(n=n, seed=s) for n, s in ((300, 7), (700, 8), (120, 9))]
