@@ -6,10 +6,12 @@
 // evaluated without FMA contraction.  The execution model is not:
 //
 //  * a group of LPP lanes (4/8/16/32) works on one pair; a block holds 128/LPP groups and the grid
-//    strides over the pair list;
-//  * both hulls are staged once per pair in shared memory as float4; every support query is a
-//    strided scan by the group's lanes plus a butterfly argmax on (value desc, index asc), which
-//    reproduces the reference's strict-'>' first-index tie break;
+//    strides over the pair list.  The device step runs two passes: GJK (gjk_pass_kernel, also one
+//    lane per pair) writes the pairs in contact with the simplex it stopped on to a list, and EPA
+//    with the force (epa_pass_kernel) continues from that list with its own lanes per pair;
+//  * a support query is a strided scan of the float4 hull vertices (staged in shared memory, or read
+//    in place from the L1-cached vertex table) by the group's lanes, then a group argmax on (value
+//    desc, index asc), which reproduces the reference's strict-'>' first-index tie break;
 //  * the simplex logic runs redundantly (identically) on every lane of the group, so control flow
 //    stays group-uniform;
 //  * EPA keeps an append-only face list of MWD_EPA_FACE_CAP faces in shared memory (the reference's
