@@ -483,6 +483,9 @@ class Simulator:
         if self.inlet is not None:
             raise ValueError("capture_host: the inlet runs inside mwd_step; use step_host without capture")
         hb = host["_buffer"]
+        if hb.device.type != "cpu" or not hb.is_pinned() or hb.dtype != self.mutable.dtype or \
+                hb.numel() != self.mutable.numel():
+            raise ValueError("capture_host: `host` must come from this simulator's host_state()")
         self.step_host(host, 1)  # warm-up outside capture
         torch.cuda.synchronize()
         npos = self.t["pos"].numel() * self.t["pos"].element_size()

@@ -120,6 +120,8 @@ def test_host_graph_matches_device_stepping():
     assert a.steps_done == 7
     for k in a.MUTABLE:
         assert torch.equal(host[k], b.t[k].cpu()), k
+    with pytest.raises(ValueError):
+        a.capture_host({"_buffer": torch.zeros(16, dtype=torch.uint8).pin_memory()})
 
 
 def test_snapshot_resume_continues_identically(tmp_path):
