@@ -309,18 +309,27 @@ def main():
     window.restore()
     host = sim.host_state()
     nbytes = sim.host_state_bytes()
+    ne = max(1, args.e2e_steps)
+
+    def host_steps():
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(ne):
+            sim.step_host(host, 1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    # for comparison: copy in, the step graph, copy out, one after another
+    sim.step_host(host, 1)
+    torch.cuda.synchronize()
+    plain_value, _ = job_rate(host_steps(), N_PARTICLES * ne, world, "cuda")
     sim.capture_host(host)
     sim.step_host(host, 1)
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ne = max(1, args.e2e_steps)
-    e0.record(stream)
-    for _ in range(ne):
-        sim.step_host(host, 1)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_value, _ = job_rate(e0.elapsed_time(e1), N_PARTICLES * ne, world, "cuda")
-    e2e = {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+    e2e_value, _ = job_rate(host_steps(), N_PARTICLES * ne, world, "cuda")
+    e2e = {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+           "copies_around_step_graph": plain_value}
 
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
