@@ -404,12 +404,19 @@ __device__ __forceinline__ void place(const BroadArgs& a, int i, int v, int g)
 __device__ __forceinline__ int order_row(const BroadArgs& a, int r)
 {
     if (r >= a.row_hi) return -1;
+    // the row's own centre, loaded beside its cell lookups (most rows are alone in their cell)
+    double4 pr = make_double4(0.0, 0.0, 0.0, 0.0);
+    if (a.sorted_pos) pr = reinterpret_cast<const double4*>(a.pos)[r];
     const int g = a.cell_of[r];
     if (g < 0) return -1;
     const int s = a.cell_start[g], e = a.cell_start[g + 1];
     const int k = e - s;
     if (k == 1) {
-        place(a, s, r, g);
+        a.sorted[s] = r;
+        if (a.sorted_pos) {
+            a.sorted_pos[s] = make_float4((float)pr.x, (float)pr.y, (float)pr.z, (float)pr.w);
+            a.sorted_cell[s] = g;
+        }
         return -1;
     }
     for (int j = s; j < e; ++j)
