@@ -55,8 +55,9 @@ class host_prints_to_stderr:
 
 METRIC = "particle-steps/s"
 WINDOW_STEPS = 500  # the pour configuration runs 500 steps
-# DRAM bytes (read + write) of one GJK-pass and one EPA-pass launch of this step, from the ncu capture
-# summarised in profiles/step_kernels_pour20k.md (5.180 MB + 0.163 MB; writes stay in L2)
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one GJK-pass and one EPA-pass
+# launch of this step, from one capture of the eager first step: 5.180 MB + 0.163 MB (the writes stay
+# in L2).  ncu cannot run inside this timing, so the figure is carried here.
 NARROW_DRAM_BYTES_PER_LAUNCH = 5.179648e6 + 0.163328e6
 # broad phase 5 (assign, cell scan, scatter, order, append) + GJK pass + EPA pass + integrator rows
 # + vertices
@@ -415,7 +416,8 @@ def breakdown(sim, V, flush, reps=10):
         roof = {"kernel": "gjk_pass_kernel + epa_pass_kernel", "bound": "fp32", "achieved": a, "peak": fp32_peak,
                 "unit": "TFLOP/s", "frac": a / fp32_peak if fp32_peak else None,
                 "traffic": NARROW_DRAM_BYTES_PER_LAUNCH,
-                "traffic_source": "profiles/step_kernels_pour20k.md (ncu dram__bytes_read + write, one launch each)",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch of each pass of the "
+                                  "eager first step (not measured in this run)",
                 "note": "latency-bound: ~13k candidate pairs, each a chain of dependent support queries; the "
                         "GJK pass issues on ~40% of cycles, the EPA pass waits on its few longest pairs",
                 "peak_source": "measured in this run (mwd_probe_fp32: FMUL+FADD chains, no FMA)"}

@@ -129,15 +129,18 @@ int mwd_contact_pairs(int64_t n_pairs, int32_t V, int32_t n_particles,
                       mwd_stream_t stream);
 
 /* The same narrow phase + contact force as mwd_contact_pairs, same arguments and results, for
- * callers that cannot allocate device memory: code running while a CUDA stream is being captured
- * (an allocation would break the capture), host frameworks that own every device allocation, and
- * processes with a fixed memory budget.  No counterpart in the reference (which allocates and
- * copies on every call).  Its scratch (17 bytes per pair, for the stride-1 history staging) is a
- * fixed array compiled into the library: at most MWD_NOALLOC_MAX_PAIRS pairs per call (larger calls
- * return MWD_ERR_INVALID); every GPU that loads the library holds the array (~4.5 MB) until the
- * process exits; all calls share it, so calls that overlap on the GPU race and must be ordered by
- * the caller.  The first call on a device looks up the array's address with that device current;
- * make that first call before any stream capture.  Calls no allocating routine. */
+ * callers that cannot let this library allocate device memory: a host application whose own
+ * allocator owns (nearly) all of the GPU's memory, so that a cudaMalloc from inside the library
+ * would fail or bypass its accounting; a process given a fixed slice of device memory up front; and
+ * a loop that cannot take the device-wide stall of the cudaFree that mwd_contact_pairs makes when
+ * its scratch grows.  No counterpart in the reference (which allocates and copies on every call).
+ * Its scratch (17 bytes per pair, for the stride-1 history staging) is a fixed array compiled into
+ * the library, 4,456,448 bytes (4.25 MiB): at most MWD_NOALLOC_MAX_PAIRS pairs per call (larger calls
+ * return MWD_ERR_INVALID); every GPU that loads the library holds the array until the process exits;
+ * all calls share it and it keeps the last call's contents, so calls that overlap on the GPU race
+ * and must be ordered by the caller.  The first call on a device looks up the array's address with
+ * that device current; make that first call before any stream capture.  Calls no cudaMalloc,
+ * cudaFree or other allocating routine. */
 #define MWD_NOALLOC_MAX_PAIRS (1 << 18)
 int mwd_contact_pairs_noalloc(int64_t n_pairs, int32_t V, int32_t n_particles,
                               const float* A_com, const float* B_com, const float* A_verts, const float* B_verts,

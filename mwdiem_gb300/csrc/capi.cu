@@ -9,6 +9,7 @@
 #include <stdarg.h>
 #include <stdio.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -38,16 +39,18 @@ int cuda_check(cudaError_t e, const char* what)
 
 int num_sms()
 {
-    static int cache[64] = {0};
+    static std::atomic<int> cache[64];
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) return 152;
-    if (!cache[dev]) {
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (!v) {
         int n = 0;
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        cache[dev] = n > 0 ? n : 152;
+        v = n > 0 ? n : 152;
+        cache[dev].store(v, std::memory_order_relaxed);
     }
-    return cache[dev];
+    return v;
 }
 
 namespace {
@@ -145,13 +148,39 @@ struct SideStream {
     cudaEvent_t fork = nullptr, join = nullptr;
     int prio_high = 0;
 };
-thread_local SideStream g_side[64];
+// Destroys a thread's streams and events when the thread exits (a pool of short-lived host threads
+// would otherwise leave one stream and two events per thread and device behind).  At process exit
+// the runtime may already be unloaded; the calls then fail harmlessly and their errors are cleared.
+struct SideStreams {
+    SideStream dev[64];
+    ~SideStreams()
+    {
+        int cur = -1;
+        if (cudaGetDevice(&cur) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        for (int d = 0; d < 64; ++d) {
+            SideStream& ss = dev[d];
+            if (!ss.s) continue;
+            if (cudaSetDevice(d) == cudaSuccess) {
+                cudaEventDestroy(ss.fork);
+                cudaEventDestroy(ss.join);
+                cudaStreamDestroy(ss.s);
+            }
+            ss = SideStream();
+        }
+        cudaSetDevice(cur);
+        cudaGetLastError();
+    }
+};
+thread_local SideStreams g_side;
 
 const SideStream* side_stream(cudaStream_t main)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-    SideStream& ss = g_side[dev];
+    SideStream& ss = g_side.dev[dev];
     if (ss.s) return &ss;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(main, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return nullptr;

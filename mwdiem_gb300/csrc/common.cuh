@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "../../include/mwdem.h"
 
 namespace mwd {
@@ -156,3 +158,42 @@ cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
         cudaError_t e_ = (call);                                        \
         if (e_ != cudaSuccess) return ::mwd::cuda_check(e_, #call);     \
     } while (0)
+
+namespace mwd {
+
+// Launch set-up of one kernel, per device: the raised dynamic shared-memory limit (a property of the
+// function on the device that was current when it was set) and the resident blocks per SM for the
+// last shared-memory size asked for.  Each is queried once per device and size, so that launches made
+// during stream capture issue no other runtime calls; a mutex guards calls from several host threads.
+struct LaunchSetup {
+    std::mutex mu;
+    bool attr[64] = {};
+    size_t shm[64] = {};
+    int per_sm[64] = {};
+};
+
+template <typename... KArgs>
+int launch_setup(LaunchSetup& c, void (*kernel)(KArgs...), int threads, size_t shm, size_t shm_limit, int* per_sm)
+{
+    int dev = 0;
+    MWD_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_error("device ordinal %d out of range", dev);
+        return MWD_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (shm_limit && !c.attr[dev]) {
+        MWD_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm_limit));
+        c.attr[dev] = true;
+    }
+    if (c.shm[dev] != shm || !c.per_sm[dev]) {
+        int v = 0;
+        MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, threads, shm));
+        c.per_sm[dev] = v < 1 ? 1 : v;
+        c.shm[dev] = shm;
+    }
+    *per_sm = c.per_sm[dev];
+    return MWD_OK;
+}
+
+}  // namespace mwd

@@ -1138,28 +1138,13 @@ template <int LPP, int ELPP>
 int launch_two_pass_lpp(const NarrowArgs& a, cudaStream_t s)
 {
     constexpr int GPB = NARROW_THREADS / ELPP;
-    // occupancy queried once per (kernel, shared-memory size); no runtime calls during capture after that
-    static int gjk_per_sm = 0;
-    static size_t epa_shm_cached = 0;
-    static int epa_per_sm = 0;
-    static bool attr = false;
-    if (!gjk_per_sm) {
-        int v = 0;
-        MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, gjk_pass_kernel<LPP>, NARROW_THREADS, 0));
-        gjk_per_sm = v < 1 ? 1 : v;
-    }
+    static LaunchSetup gjk_setup, epa_setup;
+    int gjk_per_sm = 0, epa_per_sm = 0;
+    int rc = launch_setup(gjk_setup, gjk_pass_kernel<LPP>, NARROW_THREADS, 0, 0, &gjk_per_sm);
+    if (rc) return rc;
     const size_t shm = (size_t)GPB * sizeof(EpaMem) + (a.epa_global ? 0 : (size_t)GPB * 2 * a.hull_cap * sizeof(float4));
-    if (!attr) {
-        MWD_CUDA(cudaFuncSetAttribute(epa_pass_kernel<ELPP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      200 * 1024));
-        attr = true;
-    }
-    if (shm != epa_shm_cached || !epa_per_sm) {
-        int v = 0;
-        MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, epa_pass_kernel<ELPP>, NARROW_THREADS, shm));
-        epa_per_sm = v < 1 ? 1 : v;
-        epa_shm_cached = shm;
-    }
+    rc = launch_setup(epa_setup, epa_pass_kernel<ELPP>, NARROW_THREADS, shm, 200 * 1024, &epa_per_sm);
+    if (rc) return rc;
     if (!a.epa_zeroed) MWD_CUDA(cudaMemsetAsync(a.epa_count, 0, sizeof(int32_t), s));
     if (a.hist_keys) MWD_CUDA(launch_pdl(hist_clear_kernel, (unsigned)(num_sms() * 4), 256, 0, s, a));
     MWD_CUDA(launch_pdl(gjk_pass_kernel<LPP>, (unsigned)(num_sms() * gjk_per_sm), NARROW_THREADS, 0, s, a));
@@ -1189,22 +1174,10 @@ int launch_lpp(const NarrowArgs& a, int64_t n_hint, cudaStream_t s)
 {
     constexpr int GPB = NARROW_THREADS / LPP;
     size_t shm = (size_t)GPB * sizeof(EpaMem) + (size_t)GPB * 2 * a.hull_cap * sizeof(float4);
-    // attribute and occupancy are queried once per shared-memory size, so that launches made
-    // during CUDA-graph capture issue no other runtime calls
-    static bool attr_set = false;
-    static size_t cached_shm = 0;
-    static int cached_per_sm = 0;
-    if (!attr_set) {
-        MWD_CUDA(cudaFuncSetAttribute(narrow_kernel<LPP, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        attr_set = true;
-    }
-    if (shm != cached_shm || cached_per_sm == 0) {
-        int per_sm = 0;
-        MWD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, narrow_kernel<LPP, MODE>, NARROW_THREADS, shm));
-        cached_per_sm = per_sm < 1 ? 1 : per_sm;
-        cached_shm = shm;
-    }
-    const int per_sm = cached_per_sm;
+    static LaunchSetup setup;
+    int per_sm = 0;
+    int rc = launch_setup(setup, narrow_kernel<LPP, MODE>, NARROW_THREADS, shm, 200 * 1024, &per_sm);
+    if (rc) return rc;
     int64_t grid = (int64_t)num_sms() * per_sm;
     int64_t need = (n_hint + GPB - 1) / GPB;
     if (n_hint >= 0 && need < grid) grid = need > 0 ? need : 1;

@@ -1,15 +1,15 @@
 // mwd_contact_pairs_noalloc: the narrow phase + contact force over per-pair arrays (same inputs,
-// outputs and results as mwd_contact_pairs) for callers that cannot allocate device memory --
-// for example code running inside a CUDA stream capture that must not call cudaMalloc, a host
-// framework that owns every device allocation itself, or a process whose memory budget is fixed
-// up front.  The only scratch this path needs (the staging of the reference's overlapping
-// stride-1 history writes: 17 bytes per pair) lives in a fixed-size array compiled into the
-// library, so no call allocates or frees anything.
+// outputs and results as mwd_contact_pairs) for callers that cannot let this library allocate
+// device memory -- a host application whose own allocator owns (nearly) all of the GPU's memory, a
+// process given a fixed slice of device memory up front, or a loop that cannot take the device-wide
+// stall of the cudaFree that mwd_contact_pairs makes when its scratch grows.  The only scratch this
+// path needs (the staging of the reference's overlapping stride-1 history writes: 17 bytes per pair)
+// lives in a fixed-size array compiled into the library, so no call allocates or frees anything.
 //
 // Limits and sharing:
 //  * at most MWD_NOALLOC_MAX_PAIRS pairs per call; larger calls fail with MWD_ERR_INVALID;
-//  * the array belongs to every GPU that loads the library (about 4.3 MB each) until the process
-//    exits;
+//  * the array, 4,456,448 bytes (4.25 MiB), belongs to every GPU that loads the library until the
+//    process exits;
 //  * every call uses the same array and leaves its contents behind; calls that overlap on the GPU
 //    (different streams, or different host threads on one device) race on it and must be ordered
 //    by the caller;

@@ -18,7 +18,8 @@ Variants (``variant=``):
   ``"histfix"``  FP32 contact kernel with the tangential-history index ``displacement_tang[P+k]``
                  turned into ``displacement_tang[4*P+k]`` (the stride the arrays are allocated with).
 
-The reference source is read from ``/root/reference`` when it exists.  The rendered ``.cpp`` files
+The reference checkout is read from ``$MWDEM_REFERENCE_ROOT`` (else ``DEFAULT_REFERENCE_ROOT``, where the
+checkout sits on the build machine) when it exists.  The rendered ``.cpp`` files
 are kept next to the ``.so`` so that a machine without the reference checkout can still compile the
 same renderings: ``ensure_built`` falls back to compiling an existing
 rendered file.  Compiled with ``-ffp-contract=off`` because GCC on aarch64 fuses multiply-adds by
@@ -36,7 +37,10 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 REF_DIR = HERE / "_ref"
-REFERENCE_ROOT = Path(os.environ.get("MWDEM_REFERENCE_ROOT", "/root/reference"))
+# the reference checkout on the machine that renders the templates (the GPU machine has none: it
+# compiles the renderings carried along in _ref/)
+DEFAULT_REFERENCE_ROOT = "/root/reference"
+REFERENCE_ROOT = Path(os.environ.get("MWDEM_REFERENCE_ROOT") or DEFAULT_REFERENCE_ROOT)
 CONTACT_TEMPLATE = REFERENCE_ROOT / "LIBRARIES" / "gpu_fine_contact_detection.cu"
 VERLET_TEMPLATE = REFERENCE_ROOT / "LIBRARIES" / "gpu_Verlet.cu"
 
@@ -199,6 +203,14 @@ def _key(kind: str, params: dict, variant: str) -> str:
     blob = json.dumps({"kind": kind, "variant": variant, "params": {k: _fmt(v) for k, v in sorted(params.items())}},
                       sort_keys=True)
     return hashlib.sha1(blob.encode()).hexdigest()[:16]
+
+
+def set_reference_root(path) -> None:
+    """Read the reference templates from the checkout at `path` instead."""
+    global REFERENCE_ROOT, CONTACT_TEMPLATE, VERLET_TEMPLATE
+    REFERENCE_ROOT = Path(path)
+    CONTACT_TEMPLATE = REFERENCE_ROOT / "LIBRARIES" / "gpu_fine_contact_detection.cu"
+    VERLET_TEMPLATE = REFERENCE_ROOT / "LIBRARIES" / "gpu_Verlet.cu"
 
 
 def reference_available() -> bool:

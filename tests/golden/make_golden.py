@@ -1,8 +1,9 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a checkout that has the reference at /root/reference (or $MWDEM_REFERENCE_ROOT):
+Run where the reference checkout exists; its location comes from the first argument, else from
+$MWDEM_REFERENCE_ROOT, else from oracle/build_ref.py's default:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [REFERENCE_ROOT]
 
 Sources of truth (nothing here is restated by hand except the 3-line wall test):
   * contact_*.npz  -- the reference's contact_detection kernel (LIBRARIES/gpu_fine_contact_detection.cu)
@@ -55,6 +56,8 @@ def contact_inputs():
 
 
 def main():
+    if len(sys.argv) > 1:
+        build_ref.set_reference_root(sys.argv[1])
     if not build_ref.reference_available():
         raise SystemExit("reference checkout not found")
     inp, N = contact_inputs()
