@@ -47,7 +47,8 @@ enum {
     MWD_ST_HIST_OVERFLOW = 1024u   /* persistent history: more contacts than the history table holds */
 };
 
-#define MWD_EPA_FACE_CAP 128   /* append-only EPA face list per pair */
+#define MWD_EPA_FACE_CAP 128   /* live EPA faces per pair (the list is compacted as faces are deleted) */
+#define MWD_EPA_COUNT_INTS 8   /* ints of mwd_work.epa_count */
 #define MWD_EPA_VERT_CAP 32    /* EPA polytope vertices per pair (4 + 25 iterations + 1) */
 #define MWD_HULL_CAP 64        /* hull vertices per side staged in shared memory */
 #define MWD_CELL_CAP 306       /* members per cell handled by the CPython set-order emulation */
@@ -289,7 +290,10 @@ typedef struct {
     int32_t* collision;    /* (pair_cap,) optional contact flags (NULL to skip) */
     uint64_t* work_counters; /* optional (3,), added to by the narrow phase: vertex dot products of the
                               support queries, EPA faces created, support queries (NULL: not counted) */
-    int32_t* epa_count;    /* (1,) two-pass narrow phase: pairs found in contact by the GJK pass */
+    int32_t* epa_count;    /* (MWD_EPA_COUNT_INTS,) 8-byte aligned, two-pass narrow phase: [0] pairs found in
+                              contact by the GJK pass, [2..3] the EPA pass's work queue (uint64), the
+                              rest reserved; zeroed by the broad phase of mwd_step, or by
+                              mwd_narrow_force when it runs alone */
     void* epa_rec;         /* (epa_cap, 80 B): their simplex; NULL selects the single-pass kernel */
     int64_t epa_cap;
     float* sorted_pos;     /* (n,4) centre and radius of each row in cell order (used with cull_pairs) */
@@ -337,7 +341,11 @@ int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_s
  * lanes: lanes per pair of the GJK pass (1 with the two-pass kernel, 4, 8, 16, 32), plus, in bits
  * 8-15, those of the EPA pass of the two-pass kernel (0: the same); bit 16 set: the EPA pass reads
  * the hulls in place from the vertex table instead of staging them in shared memory (less shared
- * memory, more resident pairs). */
+ * memory, more resident pairs); bits 20-21 and 22-23: threads per block of the GJK and EPA passes
+ * of the two-pass kernel (0: 128, 1: 64, 2: 256). */
+#define MWD_LANES_EPA_IN_PLACE (1 << 16)
+#define MWD_LANES_GJK_BLOCK_SHIFT 20
+#define MWD_LANES_EPA_BLOCK_SHIFT 22
 int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work* work,
                      int32_t lanes, mwd_stream_t stream);
 

@@ -14,8 +14,9 @@
 //    desc, index asc), which reproduces the reference's strict-'>' first-index tie break;
 //  * the simplex logic runs redundantly (identically) on every lane of the group, so control flow
 //    stays group-uniform;
-//  * EPA keeps an append-only face list of MWD_EPA_FACE_CAP faces in shared memory (the reference's
-//    T[50]/n[50]/dist[50] overflow past 50 faces); the face scan, the visibility test, the horizon
+//  * EPA keeps a face list of MWD_EPA_FACE_CAP entries in shared memory, append-only like the
+//    reference's T[50]/n[50]/dist[50] (which overflow past 50 faces) until it would overflow, when it
+//    is compacted (deleted faces removed in order); the face scan, the visibility test, the horizon
 //    edge count (the reference's 50x50 delpair matrix, replaced by counting over the deleted-face
 //    list) and the new faces are computed lane-parallel, with ballots to keep the reference's face
 //    order;
@@ -33,13 +34,22 @@ namespace {
 constexpr int FCAP = MWD_EPA_FACE_CAP;
 constexpr int VCAP = MWD_EPA_VERT_CAP;
 
-// per-group shared memory (the hull staging area follows, 2 * hull_cap float4)
+// per-group shared memory (the hull staging area follows, 2 * hull_cap float4).  Like the reference's
+// arrays, the face list keeps deleted faces in place with distance 3e20 (.cu:541-542) and appends new
+// ones.  When it would overflow, it is compacted instead: the deleted faces leave it, keeping the
+// order of the rest, and the earliest created of them -- the only one the minimum search could still
+// choose -- is kept aside (dn, dt), with every face's creation index (fc) for the search's ties.
 struct EpaMem {
     float4 fn[FCAP];       // face normal xyz, distance
     uint32_t ft[FCAP];     // T0 | T1 << 8 | T2 << 16 | (valid + 2) << 24
+    uint16_t fc[FCAP];     // creation index of each face (its index in the reference's arrays)
     float4 pv[VCAP];       // polytope vertices
     uint16_t pab[VCAP];    // support index on A | on B << 8
     uint32_t del[FCAP];    // faces deleted in this iteration, in index order: vertices T0 T1 T2 | face << 24
+    float4 dn;             // the earliest-created face a compaction removed: normal, distance 3e20
+    uint32_t dt;           // its vertices (ft layout)
+    float4 cn;             // the face chosen in the iteration a compaction happened in, and
+    uint32_t ct;           // its vertices (ft layout)
 };
 
 __device__ __forceinline__ int ft_v(uint32_t t, int k) { return (t >> (8 * k)) & 0xff; }
@@ -81,6 +91,23 @@ __device__ __forceinline__ int group_argmax(const Group<LPP>& g, float v, int i)
     const unsigned k = fkey(v);
     const unsigned km = __reduce_max_sync(g.mask, k);
     return (int)__reduce_min_sync(g.mask, k == km ? (unsigned)i : 0xffffffffu);
+}
+
+// Work queue of the EPA pass: a 64-bit counter after the EPA record count in the block epa_count points
+// to (MWD_EPA_COUNT_INTS ints, 8-byte aligned), ints [2..3].  Zeroed with the record count before
+// each narrow phase.
+__device__ __forceinline__ unsigned long long* epa_queue(const NarrowArgs& a)
+{
+    return reinterpret_cast<unsigned long long*>(a.epa_count + 2);
+}
+
+// The next `amount` items of a queue for the calling group: its first lane takes them with one atomic.
+template <int LPP>
+__device__ __forceinline__ int64_t claim(const Group<LPP>& g, unsigned long long* next, int64_t amount)
+{
+    unsigned long long base = 0;
+    if (g.lane == 0) base = atomicAdd(next, (unsigned long long)amount);
+    return (int64_t)__shfl_sync(g.mask, base, (int)(threadIdx.x & 31) - g.lane);
 }
 
 // argmax of d.a over A and of (-d).b over B, first index on ties (.cu:55-101)
@@ -297,11 +324,65 @@ struct EpaResult {
     uint32_t status;
 };
 
+// Removes the deleted faces (valid 0, and -1 for those of this iteration) from the face list, keeping
+// the order of the others; the earliest created of the removed faces replaces the one kept aside when
+// it was created earlier (del_c: that face's creation index, uniform over the group).  Returns the
+// number of faces left.
+template <int LPP>
+__device__ __noinline__ int epa_compact(const Group<LPP>& g, EpaMem& m, int nt, uint32_t& del_c)
+{
+    const int lane0 = (int)(threadIdx.x & 31) - g.lane;
+    int nk = 0;
+    bool first = true;
+    for (int base = 0; base < nt; base += LPP) {
+        const int f = base + g.lane;
+        bool gone = false, keep = false;
+        float4 fv = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t t = 0;
+        uint16_t c = 0;
+        if (f < nt) {
+            fv = m.fn[f];
+            t = m.ft[f];
+            c = m.fc[f];
+            const int vl = ft_valid(t);
+            gone = vl == 0 || vl == -1;
+            keep = !gone;
+        }
+        const unsigned bg = g.ballot(gone), bk = g.ballot(keep);
+        g.sync();
+        if (bg && first) {
+            // the first removed face in list (= creation) order
+            const int fl = __ffs(bg) - 1;
+            const uint32_t c0 = (uint32_t)__shfl_sync(g.mask, (int)c, lane0 + fl);
+            if (c0 < del_c) {
+                if (g.lane == fl) {
+                    m.dn = make_float4(fv.x, fv.y, fv.z, 3e20f);
+                    m.dt = (t & 0x00ffffffu) | ((uint32_t)(0 + 2) << 24);
+                }
+                del_c = c0;
+            }
+            first = false;
+        }
+        if (keep) {
+            const int o = nk + __popc(bk & g.lt_mask());
+            if (o != f) {
+                m.fn[o] = fv;
+                m.ft[o] = t;
+                m.fc[o] = c;
+            }
+        }
+        nk += __popc(bk);
+    }
+    g.sync();
+    return nk;
+}
+
 template <int LPP>
 __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, const float4* hB, int nB,
                     f3 S1, int a1, int b1, f3 S2, int a2, int b2, f3 S3, int a3, int b3, f3 S4, int a4, int b4,
                     EpaResult& r, Work3& wk)
 {
+    constexpr uint32_t NONE = 0xffffffffu;
     r.status = 0;
     g.sync();
     if (g.lane == 0) {
@@ -314,15 +395,21 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
         // faces (0,1,2), (1,2,3), (2,0,3), (0,1,3), packed as 4-bit vertex numbers (no local array)
         const unsigned long long e = 0x310302321210ull >> (12 * g.lane);
         add_face(m, (int)(e & 0xf), (int)((e >> 4) & 0xf), (int)((e >> 8) & 0xf), g.lane);
+        m.fc[g.lane] = (uint16_t)g.lane;
     }
     g.sync();
     wk.faces += 4;
-    int nt = 4, nv = 4, counter = 0, indmin = 0;
+    int nt = 4, nv = 4, counter = 0;
+    // indmin: the face chosen (>= 0: list index; -1: the face kept aside, m.dn; -2: the chosen face
+    // saved before a compaction, m.cn)
+    int indmin = 0;
+    uint32_t created = 4;
+    uint32_t del_c = NONE;  // creation index of the face in m.dn (NONE: no compaction yet)
     float xmin_old = 1e29f;
     float proj = 2 * xmin_old + 1;
     float xmin_new = 0.f;
     while (xmin_old < proj) {
-        // first index of the minimum distance
+        // array_min_finder (.cu:41-53): first index of the minimum distance over every face created
         float bv = __int_as_float(0x7fffffff);
         int bi = 0x7fffffff;
         for (int f = g.lane; f < nt; f += LPP) {
@@ -335,9 +422,23 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
             const unsigned km = __reduce_min_sync(g.mask, k);
             bi = (int)__reduce_min_sync(g.mask, k == km ? (unsigned)bi : 0xffffffffu);
         }
-        float d0 = m.fn[0].w;
-        indmin = (d0 != d0) ? 0 : bi;
-        float4 fm = m.fn[indmin];
+        if (del_c == NONE) {
+            // the search starts from face 0's distance: a NaN there keeps face 0
+            float d0 = m.fn[0].w;
+            indmin = (d0 != d0) ? 0 : bi;
+        } else {
+            // after a compaction the faces it removed (all at 3e20) are represented by the earliest
+            // created of them: it wins when no listed face is closer, or an equally close one was
+            // created later; face 0 is at the head of the list as long as it has not been removed
+            indmin = bi;
+            if (bi == 0x7fffffff) indmin = -1;
+            else {
+                const float lv = m.fn[bi].w;
+                if (lv > 3e20f || (lv == 3e20f && del_c < (uint32_t)m.fc[bi])) indmin = -1;
+            }
+            if (m.fc[0] == 0 && m.fn[0].w != m.fn[0].w) indmin = 0;
+        }
+        const float4 fm = indmin >= 0 ? m.fn[indmin] : m.dn;
         xmin_new = fm.w;
         xmin_old = xmin_new;
         f3 n = xyz(fm);
@@ -374,10 +475,28 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
             ndel += __popc(b);
         }
         g.sync();
+        // the new faces (at most three per deleted face) might not fit: compact the list first
+        const bool compacted = nt + 3 * ndel > FCAP;
+        if (compacted) {
+            if (indmin >= 0) {
+                if (g.lane == 0) {
+                    m.cn = m.fn[indmin];
+                    m.ct = m.ft[indmin];
+                }
+                indmin = -2;
+            } else if (indmin == -1) {
+                if (g.lane == 0) {
+                    m.cn = m.dn;
+                    m.ct = m.dt;
+                }
+                indmin = -2;
+            }
+            g.sync();
+            nt = epa_compact<LPP>(g, m, nt, del_c);
+        }
         // horizon edges of the deleted faces, in face order then edge order (0,1),(1,2),(2,0);
         // an edge is kept when fewer than two delpair increments land on it (.cu:482-544)
         int nnew = 0;
-        bool overflow = false;
         for (int base = 0; base < 3 * ndel; base += LPP) {
             int c = base + g.lane;
             bool keep = false;
@@ -398,21 +517,28 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
             }
             unsigned b = g.ballot(keep);
             if (keep) {
-                int f = nt + nnew + __popc(b & g.lt_mask());
-                if (f < FCAP) add_face(m, e0, e1, nv - 1, f);
+                const int q = nnew + __popc(b & g.lt_mask());
+                const int f = nt + q;
+                if (f < FCAP) {
+                    add_face(m, e0, e1, nv - 1, f);
+                    m.fc[f] = (uint16_t)(created + (uint32_t)q);
+                }
             }
             nnew += __popc(b);
         }
-        if (nt + nnew > FCAP) overflow = true;
         g.sync();
-        for (int k = g.lane; k < ndel; k += LPP) {
-            int f = (int)(m.del[k] >> 24);
-            m.ft[f] = (m.ft[f] & 0x00ffffffu) | ((uint32_t)(0 + 2) << 24);
-            m.fn[f].w = 3e20f;
+        if (!compacted) {
+            // the deleted faces stay in the list (.cu:539-542)
+            for (int k = g.lane; k < ndel; k += LPP) {
+                int f = (int)(m.del[k] >> 24);
+                m.ft[f] = (m.ft[f] & 0x00ffffffu) | ((uint32_t)(0 + 2) << 24);
+                m.fn[f].w = 3e20f;
+            }
+            g.sync();
         }
-        g.sync();
-        if (overflow) { r.status |= MWD_ST_EPA_OVERFLOW; break; }
+        if (nt + nnew > FCAP) { r.status |= MWD_ST_EPA_OVERFLOW; break; }
         nt += nnew;
+        created += (uint32_t)nnew;
         wk.faces += (uint32_t)nnew;
         counter = counter + 1;
     }
@@ -421,9 +547,10 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
     // the contact point and everything after it (the force) are needed by one lane only: the others
     // skip them, which keeps their FP64 operations (below and in contact_force) off the FP64 pipe
     if (g.lane != 0) return;
-    uint32_t t = m.ft[indmin];
+    const uint32_t t = indmin >= 0 ? m.ft[indmin] : indmin == -1 ? m.dt : m.ct;
+    const float4 fn = indmin >= 0 ? m.fn[indmin] : indmin == -1 ? m.dn : m.cn;
     int a = ft_v(t, 0), b = ft_v(t, 1), c = ft_v(t, 2);
-    f3 n = xyz(m.fn[indmin]);
+    f3 n = xyz(fn);
     f3 Pr = n * r.depth;
     f3 Va = xyz(m.pv[a]), Vb = xyz(m.pv[b]), Vc = xyz(m.pv[c]);
     f3 v0 = Vb - Va, v1 = Vc - Va, v2 = Pr - Va;
@@ -952,14 +1079,15 @@ __device__ __forceinline__ void gjk_candidates(const NarrowArgs& a, const Group<
     }
 }
 
-// one lane per pair: registers capped for 7 blocks of 128 threads per SM (the 256-scene step
-// measured 0.716 ms at 7, 0.720 at 8 and 0.726 at 6 blocks)
-template <int LPP>
-__global__ void __launch_bounds__(NARROW_THREADS, LPP == 1 ? 7 : 6) gjk_pass_kernel(NarrowArgs a)
+// BT threads per block (64, 128 or 256: the autotuner's block-size knob), registers capped so that
+// 896 threads per SM stay resident with one lane per pair (the 256-scene step measured 0.716 ms at
+// 7 blocks of 128, 0.720 at 8 and 0.726 at 6) and 768 with lane groups
+template <int LPP, int BT>
+__global__ void __launch_bounds__(BT, (LPP == 1 ? 896 : 768) / BT) gjk_pass_kernel(NarrowArgs a)
 {
     pdl_wait();
     pdl_launch_dependents();
-    constexpr int GPB = NARROW_THREADS / LPP;
+    constexpr int GPB = BT / LPP;
     const int grp = threadIdx.x / LPP;
     Group<LPP> g;
     g.lane = threadIdx.x % LPP;
@@ -1114,14 +1242,18 @@ __device__ __forceinline__ void epa_record(const NarrowArgs& a, const Group<LPP>
     g.sync();
 }
 
-// registers capped for 5 blocks of 128 threads per SM
-template <int LPP>
-__global__ void __launch_bounds__(NARROW_THREADS, 5) epa_pass_kernel(NarrowArgs a)
+// the EPA queue's smallest claim, and the fraction of the remaining records per group a claim takes
+constexpr int EPA_CLAIM = 2;
+constexpr int EPA_GUIDE = 4;
+
+// BT threads per block, registers capped so that 640 threads per SM stay resident (5 blocks of 128)
+template <int LPP, int BT>
+__global__ void __launch_bounds__(BT, 640 / BT) epa_pass_kernel(NarrowArgs a)
 {
     pdl_wait();
     pdl_launch_dependents();
     extern __shared__ float4 smem[];
-    constexpr int GPB = NARROW_THREADS / LPP;
+    constexpr int GPB = BT / LPP;
     const int grp = threadIdx.x / LPP;
     Group<LPP> g;
     g.lane = threadIdx.x % LPP;
@@ -1129,28 +1261,78 @@ __global__ void __launch_bounds__(NARROW_THREADS, 5) epa_pass_kernel(NarrowArgs 
     EpaMem* em = reinterpret_cast<EpaMem*>(smem) + grp;
     float4* hull = reinterpret_cast<float4*>(reinterpret_cast<EpaMem*>(smem) + GPB) + (size_t)grp * 2 * a.hull_cap;
     const int cnt = *a.epa_count;
-    const int64_t m = cnt < a.epa_cap ? cnt : a.epa_cap;
-    for (int64_t i = (int64_t)blockIdx.x * GPB + grp; i < m; i += (int64_t)gridDim.x * GPB)
+    const int m = (int64_t)cnt < a.epa_cap ? cnt : (int)a.epa_cap;
+    // Persistent over a work queue (guided self-scheduling): every group first takes a fixed share of
+    // the records, interleaved with the others' (all of them when there are no more records than
+    // groups: no atomic at all); the rest are claimed from the queue in pieces of a quarter of what is
+    // left per group, so that the groups that finish early take over the work of the others and the
+    // pass ends with its last record rather than with the unluckiest fixed share.  (Record counts are
+    // int32.)
+    const int G = (int)gridDim.x * GPB;
+    const int share = m <= G ? 1 : (m / (2 * G) > 1 ? m / (2 * G) : 1);
+    const int fixed = m <= G ? m : G * share;
+    unsigned long long* next = epa_queue(a);
+    // records i, i + step, ... below e: first the fixed share (step G), then each claimed piece (step 1)
+    int i = (int)blockIdx.x * GPB + grp, step = G, e = fixed;
+    int seen = 0;  // queue position after this group's last claim
+    for (;;) {
+        if (i >= e) {
+            if (fixed >= m) break;
+            int size = (m - fixed - seen) / (EPA_GUIDE * G);
+            if (size < EPA_CLAIM) size = EPA_CLAIM;
+            const int64_t b = (int64_t)fixed + claim<LPP>(g, next, size);
+            if (b >= m) break;
+            i = (int)b;
+            step = 1;
+            e = b + size < m ? (int)b + size : m;
+            seen = i - fixed + size;
+        }
         epa_record<LPP>(a, g, em, hull, i);
+        i += step;
+    }
 }
 
-template <int LPP, int ELPP>
-int launch_two_pass_lpp(const NarrowArgs& a, cudaStream_t s)
+// threads per block of a block-size code of the lanes word (0: 128, 1: 64, 2: 256)
+inline int block_threads(int code) { return code == 1 ? 64 : code == 2 ? 256 : 128; }
+
+template <int LPP, int BT>
+int launch_gjk_bt(const NarrowArgs& a, cudaStream_t s)
 {
-    constexpr int GPB = NARROW_THREADS / ELPP;
-    static LaunchSetup gjk_setup, epa_setup;
-    int gjk_per_sm = 0, epa_per_sm = 0;
-    int rc = launch_setup(gjk_setup, gjk_pass_kernel<LPP>, NARROW_THREADS, 0, 0, &gjk_per_sm);
+    static LaunchSetup setup;
+    int per_sm = 0;
+    int rc = launch_setup(setup, gjk_pass_kernel<LPP, BT>, BT, 0, 0, &per_sm);
     if (rc) return rc;
-    const size_t shm = (size_t)GPB * sizeof(EpaMem) + (a.epa_global ? 0 : (size_t)GPB * 2 * a.hull_cap * sizeof(float4));
-    rc = launch_setup(epa_setup, epa_pass_kernel<ELPP>, NARROW_THREADS, shm, 200 * 1024, &epa_per_sm);
-    if (rc) return rc;
-    if (!a.epa_zeroed) MWD_CUDA(cudaMemsetAsync(a.epa_count, 0, sizeof(int32_t), s));
-    if (a.hist_keys) MWD_CUDA(launch_pdl(hist_clear_kernel, (unsigned)(num_sms() * 4), 256, 0, s, a));
-    MWD_CUDA(launch_pdl(gjk_pass_kernel<LPP>, (unsigned)(num_sms() * gjk_per_sm), NARROW_THREADS, 0, s, a));
-    MWD_CUDA(launch_pdl(epa_pass_kernel<ELPP>, (unsigned)(num_sms() * epa_per_sm), NARROW_THREADS, shm, s, a));
-    if (a.hist_keys) MWD_CUDA(launch_pdl(hist_flip_kernel, 1, 32, 0, s, a));
+    MWD_CUDA(launch_pdl(gjk_pass_kernel<LPP, BT>, (unsigned)(num_sms() * per_sm), BT, 0, s, a));
     return MWD_OK;
+}
+
+template <int LPP>
+int launch_gjk(const NarrowArgs& a, int code, cudaStream_t s)
+{
+    if (code == 1) return launch_gjk_bt<LPP, 64>(a, s);
+    if (code == 2) return launch_gjk_bt<LPP, 256>(a, s);
+    return launch_gjk_bt<LPP, 128>(a, s);
+}
+
+template <int LPP, int BT>
+int launch_epa_bt(const NarrowArgs& a, cudaStream_t s)
+{
+    constexpr int GPB = BT / LPP;
+    static LaunchSetup setup;
+    int per_sm = 0;
+    const size_t shm = (size_t)GPB * sizeof(EpaMem) + (a.epa_global ? 0 : (size_t)GPB * 2 * a.hull_cap * sizeof(float4));
+    int rc = launch_setup(setup, epa_pass_kernel<LPP, BT>, BT, shm, 200 * 1024, &per_sm);
+    if (rc) return rc;
+    MWD_CUDA(launch_pdl(epa_pass_kernel<LPP, BT>, (unsigned)(num_sms() * per_sm), BT, shm, s, a));
+    return MWD_OK;
+}
+
+template <int LPP>
+int launch_epa(const NarrowArgs& a, int code, cudaStream_t s)
+{
+    if (code == 1) return launch_epa_bt<LPP, 64>(a, s);
+    if (code == 2) return launch_epa_bt<LPP, 256>(a, s);
+    return launch_epa_bt<LPP, 128>(a, s);
 }
 
 // Resolve the reference's overlapping stride-1 history writes (.cu:1018-1021, :1158-1161): the
@@ -1215,22 +1397,45 @@ int launch_narrow(const NarrowArgs& a, int mode, int lanes, int64_t n_hint, cuda
     return MWD_ERR_INVALID;
 }
 
-// lanes = GJK-pass lanes per pair | EPA-pass lanes per pair << 8 (EPA lanes 0: same as GJK); whether
-// the EPA pass reads the hulls in place comes in NarrowArgs (epa_global)
+// lanes = GJK-pass lanes per pair | EPA-pass lanes per pair << 8 (EPA lanes 0: same as GJK) | the two
+// passes' block-size codes (MWD_LANES_*_BLOCK_SHIFT); whether the EPA pass reads the hulls in place
+// comes in NarrowArgs (epa_global)
 int launch_narrow_two_pass(const NarrowArgs& a, int lanes, cudaStream_t s)
 {
     const int gl = lanes & 0xff;
     int el = (lanes >> 8) & 0xff;
     if (!el) el = gl;
-#define MWD_TP(G, E) if (gl == G && el == E) return launch_two_pass_lpp<G, E>(a, s)
-    MWD_TP(1, 4); MWD_TP(1, 8); MWD_TP(1, 16); MWD_TP(1, 32);
-    MWD_TP(4, 4); MWD_TP(4, 8); MWD_TP(4, 16); MWD_TP(4, 32);
-    MWD_TP(8, 8); MWD_TP(8, 16); MWD_TP(8, 32); MWD_TP(8, 4);
-    MWD_TP(16, 16); MWD_TP(16, 32); MWD_TP(16, 8); MWD_TP(16, 4);
-    MWD_TP(32, 32); MWD_TP(32, 16); MWD_TP(32, 8); MWD_TP(32, 4);
-#undef MWD_TP
-    set_error("lanes per pair must be 1 (GJK pass only), 4, 8, 16 or 32 (got GJK %d, EPA %d)", gl, el);
-    return MWD_ERR_INVALID;
+    const int gb = (lanes >> MWD_LANES_GJK_BLOCK_SHIFT) & 3, eb = (lanes >> MWD_LANES_EPA_BLOCK_SHIFT) & 3;
+    const bool gl_ok = gl == 1 || gl == 4 || gl == 8 || gl == 16 || gl == 32;
+    const bool el_ok = el == 4 || el == 8 || el == 16 || el == 32;
+    if (!gl_ok || !el_ok) {
+        set_error("lanes per pair must be 1 (GJK pass only), 4, 8, 16 or 32 (got GJK %d, EPA %d)", gl, el);
+        return MWD_ERR_INVALID;
+    }
+    if (gb == 3 || eb == 3) {
+        set_error("block-size code must be 0 (128 threads), 1 (64) or 2 (256) (got GJK %d, EPA %d)", gb, eb);
+        return MWD_ERR_INVALID;
+    }
+    if (!a.epa_zeroed) MWD_CUDA(cudaMemsetAsync(a.epa_count, 0, MWD_EPA_COUNT_INTS * sizeof(int32_t), s));
+    if (a.hist_keys) MWD_CUDA(launch_pdl(hist_clear_kernel, (unsigned)(num_sms() * 4), 256, 0, s, a));
+    int rc = MWD_OK;
+    switch (gl) {
+        case 1: rc = launch_gjk<1>(a, gb, s); break;
+        case 4: rc = launch_gjk<4>(a, gb, s); break;
+        case 8: rc = launch_gjk<8>(a, gb, s); break;
+        case 16: rc = launch_gjk<16>(a, gb, s); break;
+        default: rc = launch_gjk<32>(a, gb, s); break;
+    }
+    if (rc) return rc;
+    switch (el) {
+        case 4: rc = launch_epa<4>(a, eb, s); break;
+        case 8: rc = launch_epa<8>(a, eb, s); break;
+        case 16: rc = launch_epa<16>(a, eb, s); break;
+        default: rc = launch_epa<32>(a, eb, s); break;
+    }
+    if (rc) return rc;
+    if (a.hist_keys) MWD_CUDA(launch_pdl(hist_flip_kernel, 1, 32, 0, s, a));
+    return MWD_OK;
 }
 
 int launch_hist_resolve(float* hist, const float* stage, const uint8_t* wrote, int64_t n, cudaStream_t s)

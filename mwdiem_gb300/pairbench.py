@@ -14,7 +14,7 @@ import numpy as np
 import torch
 
 from . import scene
-from ._lib import ContactParams, Scene, State, Work, check, lib
+from ._lib import EPA_COUNT_INTS, ContactParams, Scene, State, Work, check, lib
 
 
 class PairScene:
@@ -117,7 +117,7 @@ class PairScene:
         wk.collision = w["collision"].data_ptr()
         wk.pair_cap = self.n_pairs
         if two_pass:
-            w["epa_count"] = torch.zeros(1, **i32)
+            w["epa_count"] = torch.zeros(EPA_COUNT_INTS, **i32)
             w["epa_rec"] = torch.zeros(self.n_pairs * 80, dtype=torch.uint8, device=dev)
             wk.epa_count, wk.epa_rec, wk.epa_cap = w["epa_count"].data_ptr(), w["epa_rec"].data_ptr(), self.n_pairs
         self.w = w
@@ -134,29 +134,35 @@ class PairScene:
         self.work.work_counters = None
 
     def gather(self, idx):
-        """Per-pair float32 arrays (reference layout) for the pairs `idx` (host), for the oracle."""
+        """Per-pair float32 arrays (reference layout) for the pairs `idx` (host), for the oracle.  Only
+        the rows of those pairs are copied from the device."""
         idx = np.asarray(idx)
-        t = {k: v for k, v in self.t.items()}
-        off = t["vert_off"].cpu().numpy().astype(np.int64)
-        wv = t["world_verts"].cpu().numpy()
-        a, b = 2 * idx, 2 * idx + 1
+        dev = self.t["pos"].device
+        a = torch.from_numpy(2 * idx).to(dev)
+        b = a + 1
+        off = self.t["vert_off"].long()
         V = self.V
 
         def verts(rows):
-            out = np.zeros((len(rows), V, 3), np.float32)
-            for i, r in enumerate(rows):
-                out[i, :off[r + 1] - off[r]] = wv[off[r]:off[r + 1], :3]
-            return out
-        pos = t["pos"].cpu().numpy()
-        vel = t["vel"].cpu().numpy()
-        w = t["w"].cpu().numpy()
-        q = t["q"].cpu().numpy()
-        ine = t["inertia"].cpu().numpy()
-        nv = np.diff(off).astype(np.int32)
-        return dict(A_com=pos[a, :3].astype(np.float32), B_com=pos[b, :3].astype(np.float32), A_verts=verts(a),
-                    B_verts=verts(b), A_vel=vel[a, :3], B_vel=vel[b, :3], A_angvel=w[a, :3], B_angvel=w[b, :3],
-                    A_nv=nv[a], B_nv=nv[b], A_id=a.astype(np.int32), B_id=b.astype(np.int32),
-                    hist=np.zeros((len(idx), 4), np.float32), qA=q[a], qB=q[b], IsA=ine[a, 3], IsB=ine[b, 3])
+            cnt = off[rows + 1] - off[rows]
+            ar = torch.arange(V, device=dev)
+            mask = ar[None, :] < cnt[:, None]
+            src = torch.where(mask, off[rows][:, None] + ar[None, :], torch.zeros_like(mask, dtype=torch.long))
+            out = torch.where(mask[..., None], self.t["world_verts"][src][..., :3], 0.0)
+            return out.cpu().numpy()
+
+        def rows_of(k, rows, cols=slice(0, 3)):
+            return self.t[k][rows][:, cols].cpu().numpy()
+
+        nv = (off[1:] - off[:-1]).int()
+        ai, bi = a.cpu().numpy(), b.cpu().numpy()
+        return dict(A_com=rows_of("pos", a).astype(np.float32), B_com=rows_of("pos", b).astype(np.float32),
+                    A_verts=verts(a), B_verts=verts(b), A_vel=rows_of("vel", a), B_vel=rows_of("vel", b),
+                    A_angvel=rows_of("w", a), B_angvel=rows_of("w", b), A_nv=nv[a].cpu().numpy(),
+                    B_nv=nv[b].cpu().numpy(), A_id=ai.astype(np.int32), B_id=bi.astype(np.int32),
+                    hist=np.zeros((len(idx), 4), np.float32), qA=rows_of("q", a, slice(0, 4)),
+                    qB=rows_of("q", b, slice(0, 4)), IsA=self.t["inertia"][a, 3].cpu().numpy(),
+                    IsB=self.t["inertia"][b, 3].cpu().numpy())
 
 
 def _quat_to_matrix(q):

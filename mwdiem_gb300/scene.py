@@ -333,3 +333,49 @@ def batched_scenes(n_scenes=256, total=2_000_000, n_lo=100, n_hi=50_000, seed=0,
                                 Kn=kn, en=en, et=en, mu=mu, Kn_wall=kn, en_wall=en, et_wall=en, mu_wall=mu, dt=dt,
                                 max_particlesize=2.4, name=f"batch{s}"))
     return scenes
+
+
+def reference_arrays(spec: SceneSpec, V=None, bodies=None, q0=None):
+    """The state a scene gives the reference's per-step loop: its FP64 arrays (MWDiem.py:603-646),
+    walls first, vertices in world coordinates padded with zeros to V, plus what the loop reads
+    beside them.  `bodies`/`q0` replace the scene's bodies and starting orientations (the physical
+    contact law's principal-axes frames).  Returns (state, aux): state holds v, v12, w12bf, wbf, w,
+    F, T, com, dxall, q12, q, qall, verts, mass, Iinv, I; aux holds nv (vertex counts), Is
+    (moment_of_inertia_size, Particle_class.py:151), ext (external force: gravity), wall_n, wall_c,
+    wall_range (6 max_particlesize, MWDiem.py:808-811), the cell grid (nx, ny, cs) and the box."""
+    W = spec.n_walls
+    parts = spec.body_list() if bodies is None else list(bodies)
+    all_bodies = [b for b, _, _ in spec.walls] + parts
+    centres = np.concatenate([np.array([c for _, c, _ in spec.walls]).reshape(-1, 3), np.asarray(spec.centres)], 0)
+    N = len(all_bodies)
+    nv = np.array([b.vertices.shape[0] for b in all_bodies], dtype=np.int32)
+    V = int(V or nv.max())
+    verts = np.zeros((N, V, 3))
+    for i, b in enumerate(all_bodies):
+        verts[i, :nv[i]] = centres[i] + b.vertices
+    mass = np.array([b.mass for b in all_bodies])
+    I = np.zeros((N, 3, 3))
+    Iinv = np.zeros((N, 3, 3))
+    for i, b in enumerate(all_bodies):
+        I[i] = np.diag(b.inertia_bf)
+        Iinv[i] = np.diag(1.0 / np.asarray(b.inertia_bf))
+    if q0 is None:
+        q0 = np.tile([1.0, 0.0, 0.0, 0.0], (N, 1))
+
+    def z():
+        return np.zeros((N, 3))
+
+    st = dict(v=z(), v12=z(), w12bf=z(), wbf=z(), w=z(), F=z(), T=z(), com=centres.copy(), dxall=z(),
+              q12=q0.copy(), q=q0.copy(), qall=np.tile([1.0, 0.0, 0.0, 0.0], (N, 1)), verts=verts, mass=mass,
+              Iinv=Iinv, I=I)
+    if spec.velocities is not None:
+        st["v"][W:] = spec.velocities
+        st["v12"][W:] = spec.velocities
+    ext = np.zeros((N, 3))
+    ext[W:] = mass[W:, None] * np.asarray(spec.gravity)[None, :]
+    ncell, cs = spec.grid()
+    aux = dict(nv=nv, V=V, Is=np.array([b.inertia_size for b in all_bodies]), ext=ext,
+               wall_n=np.array([n for _, _, n in spec.walls]).reshape(-1, 3), wall_c=centres[:W].copy(),
+               wall_range=6.0 * spec.max_particlesize, nx=int(ncell[0]), ny=int(ncell[1]), cs=cs, box=spec.box(),
+               W=W, N=N)
+    return st, aux

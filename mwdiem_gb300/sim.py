@@ -15,7 +15,7 @@ import numpy as np
 import torch
 
 from . import _dev
-from ._lib import (HULL_CAP, INFO_INACTIVE, LAW_PHYSICAL, LAW_REFERENCE, ST_PAIR_OVERFLOW, ContactParams, Inlet,
+from ._lib import (EPA_COUNT_INTS, HULL_CAP, INFO_INACTIVE, LAW_PHYSICAL, LAW_REFERENCE, ST_PAIR_OVERFLOW, ContactParams, Inlet,
                    Material, MwdError, Scene, State, Work, check, lib, status_names)
 from .scene import CompactBodies, SceneSpec
 
@@ -319,7 +319,7 @@ class Simulator:
         w["work_counters"] = torch.zeros(3, dtype=torch.int64, device=self.device)
         wk.work_counters = None
         if self.two_pass:
-            w["epa_count"] = torch.zeros(1, **i32)
+            w["epa_count"] = torch.zeros(EPA_COUNT_INTS, **i32)
             w["epa_rec"] = torch.zeros(cap * 80, dtype=torch.uint8, device=self.device)
             wk.epa_count = w["epa_count"].data_ptr()
             wk.epa_rec = w["epa_rec"].data_ptr()
@@ -557,10 +557,11 @@ class Simulator:
         """(n, V, 3) float32 world vertices padded with zeros, like the reference's per-pair gather."""
         off = self.vert_off_host
         wv = self.t["world_verts"].cpu().numpy()
+        cnt = off[1:] - off[:-1]
         out = np.zeros((self.n, V, 3), dtype=np.float32)
-        for r in range(self.n):
-            k = off[r + 1] - off[r]
-            out[r, :k] = wv[off[r]:off[r + 1], :3]
+        mask = np.arange(V)[None, :] < cnt[:, None]
+        src = off[:-1][:, None] + np.arange(V)[None, :]
+        out[mask] = wv[src[mask], :3]
         return out
 
     # ------------------------------------------------------------------ snapshots

@@ -23,7 +23,8 @@
 #include <string.h>
 
 #define ORC_VCAP 64
-#define ORC_FCAP 512
+#define ORC_FCAP 4096      /* faces an EPA may create (storage; the reference's T[50] overflows at 50) */
+#define ORC_LIVE_CAP 128   /* faces alive at once: the CUDA kernel's compacted list (MWD_EPA_FACE_CAP) */
 #define ORC_DIAG 19
 #define ORC_NCOUNT 10
 #define ORC_ST_EPA_NOCONV 1
@@ -37,7 +38,7 @@ typedef struct {
     double dt;
     int n_wall;
     int hist_stride4; /* 0: reference stride-1 history indexing, 1: stride 4 */
-    int face_cap;     /* EPA face-list capacity (<= ORC_FCAP); 0 -> ORC_FCAP */
+    int face_cap;     /* faces an EPA may create (<= ORC_FCAP; 50 is the reference's T[50]); 0 -> ORC_FCAP */
     int physical;     /* 1: the physical-mass contact law (effective masses, midpoint contact point) */
 } orc_contact_params;
 

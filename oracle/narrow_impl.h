@@ -13,8 +13,9 @@
  * Differences from the reference, all deliberate and mirrored by the CUDA kernel:
  *  - EPA keeps an append-only face list of ORC_FCAP faces and a vertex list of ORC_VCAP entries
  *    instead of T[50]/V[50]; the reference writes past T[50] when more than 50 faces are created
- *    (gpu_fine_contact_detection.cu:359-362,519-539).  Overflow stops the EPA and raises
- *    ORC_ST_EPA_OVERFLOW instead.
+ *    (gpu_fine_contact_detection.cu:359-362,519-539).  More than face_cap faces created (50 selects
+ *    the reference's own limit), or more than ORC_LIVE_CAP faces alive at the end of an iteration
+ *    (the CUDA kernel keeps only the live faces), stops the EPA and raises ORC_ST_EPA_OVERFLOW.
  *  - the horizon is found by counting, for each edge of each deleted face, how many increments the
  *    reference's delpair[50][50] matrix would have received (gpu_fine_contact_detection.cu:482-493),
  *    without the matrix.
@@ -232,7 +233,8 @@ static void ORC_N(epa)(V3 S1, int a1, int b1, V3 S2, int a2, int b2, V3 S3, int 
     ORC_N(face)(p, 1, 2, 3, p->nt++);
     ORC_N(face)(p, 2, 0, 3, p->nt++);
     ORC_N(face)(p, 0, 1, 3, p->nt++);
-    int del[ORC_FCAP];
+    int live = 4;
+    static ORC_THREAD int del[ORC_FCAP];
     while (xmin_old < proj) {
         /* first index of the minimum, strict '<' from dist[0] */
         indmin = 0;
@@ -261,6 +263,7 @@ static void ORC_N(epa)(V3 S1, int a1, int b1, V3 S2, int a2, int b2, V3 S3, int 
                 del[ndel++] = i;
             }
         int overflow = 0;
+        const int nt_before = p->nt;
         for (int k = 0; k < ndel && !overflow; ++k) {
             int i = del[k];
             int t0 = p->T[i][0], t1 = p->T[i][1], t2 = p->T[i][2];
@@ -276,6 +279,8 @@ static void ORC_N(epa)(V3 S1, int a1, int b1, V3 S2, int a2, int b2, V3 S3, int 
             p->dist[i] = (RT)3e20;
         }
         if (overflow) { out->status |= ORC_ST_EPA_OVERFLOW; break; }
+        live = live - ndel + (p->nt - nt_before);
+        if (live > ORC_LIVE_CAP) { out->status |= ORC_ST_EPA_OVERFLOW; break; }
         counter = counter + 1;
     }
     out->faces = p->nt;

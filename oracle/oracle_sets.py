@@ -62,6 +62,28 @@ def settling_sets():
     return dict(s.params), s.verlet_params()
 
 
+def batch_sample(specs, n_sample=8):
+    """The scenes of a batch whose reference path the batched benchmark runs: the largest, then
+    n_sample - 1 others drawn at random (seed 0)."""
+    import numpy as np
+    rng = np.random.default_rng(0)
+    first = int(np.argmax([sp.n_particles for sp in specs]))
+    rest = [i for i in range(len(specs)) if i != first]
+    return [first] + [int(i) for i in rng.choice(rest, size=min(n_sample - 1, len(rest)), replace=False)]
+
+
+def batch_sets(n_scenes=256, total=2_000_000):
+    """Contact and integrator parameter sets of the sampled scenes of the batched benchmark."""
+    import stepper
+    from mwdiem_gb300 import scene
+    specs = scene.batched_scenes(n_scenes=n_scenes, total=total, seed=0)
+    out = []
+    for i in batch_sample(specs):
+        s = stepper.RefStepper(specs[i], kind="port")
+        out.append((dict(s.params), s.verlet_params()))
+    return out
+
+
 def render_all():
     c, v = pour_sets()
     register_contact(c)
@@ -70,6 +92,9 @@ def render_all():
     c, v = settling_sets()
     register_contact(c)
     register_verlet(v)
+    for c, v in batch_sets():
+        register_contact(c)
+        register_verlet(v)
     out = []
     for p in CONTACT_SETS:
         out.append(build_ref.ensure_built("contact", p, "f32"))

@@ -17,15 +17,22 @@ from __future__ import annotations
 import numpy as np
 
 import oracle
+from mwdiem_gb300 import scene
 from mwdiem_gb300.shapes import quat_to_matrix
 
 
 class RefStepper:
-    def __init__(self, spec, V=None, kind="port", nthreads=1):
-        """spec: mwdiem_gb300.scene.SceneSpec (walls first, then particles)."""
+    def __init__(self, spec, V=None, kind="port", nthreads=1, inlet=None):
+        """spec: mwdiem_gb300.scene.SceneSpec (walls first, then particles).
+
+        inlet: optional (period, per_spawn, first_row, spawn) -- particles entering during the run
+        (MWDiem.py:685-714): rows from first_row on wait outside the broad phase and the integrator
+        (the reference's num_particles_temp bound) and, every `period` steps from step 0, the next
+        `per_spawn` of them enter at rest at their row of `spawn` ((N, 3) centres), unrotated."""
         W = spec.n_walls
         self.law = getattr(spec, "law", "reference")
         q0 = np.tile([1.0, 0.0, 0.0, 0.0], (W + spec.n_particles, 1))
+        parts = None
         if self.law == "physical":
             # principal-axes body frames and starting orientations (SceneSpec.principal_bodies)
             pb, q0[W:] = spec.principal_bodies()
@@ -33,43 +40,22 @@ class RefStepper:
             rot = [quat_to_matrix(q) for q in q0[W:]]
             parts = [type(b)(vertices=b.vertices @ R.T, inertia_bf=b.inertia_bf, inertia_size=b.inertia_size,
                              mass=b.mass) for b, R in zip(parts, rot)]
-        else:
-            parts = spec.body_list()
-        bodies = [b for b, _, _ in spec.walls] + parts
-        centres = np.concatenate([np.array([c for _, c, _ in spec.walls]).reshape(-1, 3), spec.centres], 0)
-        N = len(bodies)
-        nv = np.array([b.vertices.shape[0] for b in bodies], dtype=np.int32)
-        self.V = int(V or nv.max())
+        st, aux = scene.reference_arrays(spec, V=V, bodies=parts, q0=q0)
+        N = aux["N"]
+        self.V = aux["V"]
         V = self.V
-        verts = np.zeros((N, V, 3))
-        for i, b in enumerate(bodies):
-            verts[i, :nv[i]] = centres[i] + b.vertices
-        mass = np.array([b.mass for b in bodies])
-        I = np.zeros((N, 3, 3))
-        Iinv = np.zeros((N, 3, 3))
-        for i, b in enumerate(bodies):
-            I[i] = np.diag(b.inertia_bf)
-            Iinv[i] = np.diag(1.0 / np.asarray(b.inertia_bf))
-        z = lambda: np.zeros((N, 3))  # noqa: E731
-        q = lambda: np.tile([1.0, 0.0, 0.0, 0.0], (N, 1))  # noqa: E731
-        st = dict(v=z(), v12=z(), w12bf=z(), wbf=z(), w=z(), F=z(), T=z(), com=centres.copy(), dxall=z(),
-                  q12=q0.copy(), q=q0.copy(), qall=q(), verts=verts, mass=mass, Iinv=Iinv, I=I)
-        if spec.velocities is not None:
-            st["v"][W:] = spec.velocities
-            st["v12"][W:] = spec.velocities
+        centres = st["com"].copy()
         self.st = st
-        self.ext = np.zeros((N, 3))
-        self.ext[W:] = mass[W:, None] * np.asarray(spec.gravity)[None, :]
-        self.nv = nv
-        self.Is = np.array([b.inertia_size for b in bodies])
+        self.ext = aux["ext"]
+        self.nv = aux["nv"]
+        self.Is = aux["Is"]
         self.W = W
         self.N = N
-        self.wall_n = np.array([n for _, _, n in spec.walls]).reshape(-1, 3)
-        self.wall_range = 6.0 * spec.max_particlesize
-        ncell, cs = spec.grid()
-        self.nx, self.ny = int(ncell[0]), int(ncell[1])
-        self.cs = cs
-        self.box = spec.box()
+        self.wall_n = aux["wall_n"]
+        self.wall_range = aux["wall_range"]
+        self.nx, self.ny = aux["nx"], aux["ny"]
+        self.cs = aux["cs"]
+        self.box = aux["box"]
         self.dt = spec.dt
         self.params = dict(Kn=spec.Kn, en=spec.en, et=spec.et, mu=spec.mu, Kn_wall=spec.Kn_wall,
                            en_wall=spec.en_wall, et_wall=spec.et_wall, mu_wall=spec.mu_wall, num_vertices_max=V,
@@ -86,6 +72,33 @@ class RefStepper:
             self.ref_v = oracle.RefVerlet(vp)
         self.last_pairs = None
         self.last_collision = None
+        self.n_steps = 0
+        self.active_end = N          # rows [W, active_end) take part in the step
+        self.inlet = None
+        if inlet is not None:
+            period, per_spawn, first, spawn = inlet
+            self.inlet = (int(period), int(per_spawn), np.asarray(spawn, dtype=np.float64))
+            self.active_end = int(first)
+            self.body = [st["verts"][i] - centres[i] for i in range(N)]  # body-frame vertices (unrotated)
+
+    def _inlet_step(self):
+        """Rows entering at the start of this step (MWDiem.py:685-714)."""
+        period, per_spawn, spawn = self.inlet
+        if self.n_steps % period != 0:
+            return
+        st = self.st
+        lo, hi = self.active_end, min(self.N, self.active_end + per_spawn)
+        for r in range(lo, hi):
+            c = spawn[r]
+            for k in ("v", "v12", "w12bf", "wbf", "w", "F", "T", "dxall"):
+                st[k][r] = 0.0
+            for k in ("q", "q12", "qall"):
+                st[k][r] = (1.0, 0.0, 0.0, 0.0)
+            st["com"][r] = c
+            k = self.nv[r]
+            st["verts"][r] = 0.0
+            st["verts"][r, :k] = c + self.body[r][:k]
+        self.active_end = hi
 
     def verlet_params(self):
         return dict(timestep_size=self.dt, num_particles=self.N, num_vertices_max=self.V, syssize_x_max=self.box[0],
@@ -93,7 +106,7 @@ class RefStepper:
                     syssize_z_max=self.box[4], syssize_z_min=self.box[5], num_part_min=self.W, num_part_max=self.N)
 
     def candidate_pairs(self):
-        st, W, N = self.st, self.W, self.N
+        st, W, N = self.st, self.W, self.active_end
         wall = oracle.wall_pairs(W, W, N, st["com"], self.wall_n, st["com"][:W], self.wall_range)
         keys = oracle.cell_keys(st["com"], self.cs[0], self.cs[1], self.cs[2], self.nx, self.ny)
         cells = oracle.linked_cell_hash(W, N, keys, self.nx, self.ny)
@@ -122,7 +135,10 @@ class RefStepper:
         return im[pairs[:, 0]], im[pairs[:, 1]]
 
     def step(self):
-        st, W, N = self.st, self.W, self.N
+        if self.inlet is not None:
+            self._inlet_step()
+        st, W, N, act = self.st, self.W, self.N, self.active_end
+        self.n_steps += 1
         pairs = self.candidate_pairs()
         self.last_pairs = pairs
         if len(pairs):
@@ -142,9 +158,11 @@ class RefStepper:
         st["F"][:] = force + self.ext
         st["T"][:] = torque
         if self.kind == "reference":
+            if act != N:
+                raise ValueError("the reference's own integrator build covers every row; use kind='port' with an inlet")
             self.ref_v.run(st, nthreads=self.nthreads)
         else:
-            oracle.verlet_f64(st, self.dt, self.box, W, N, physical=self.law == "physical")
+            oracle.verlet_f64(st, self.dt, self.box, W, act, physical=self.law == "physical")
         return len(pairs)
 
 

@@ -16,8 +16,6 @@ from helpers import CONTACT_PARAMS, cube_pair_kat, make_pairs, select
 
 pytestmark = pytest.mark.gpu
 
-FACE_CAP = 128
-
 
 def run_gpu(inp, N, params, lanes=8, hist_mode=0):
     from mwdiem_gb300 import gpu_fine_contact_detection as G
@@ -55,7 +53,7 @@ def bits_equal(a, b):
 @pytest.mark.parametrize("lanes", [4, 8, 16, 32])
 def test_bitexact_vs_oracle_f32(lanes):
     inp, N = make_pairs(1500, seed=11)
-    o = oracle.contact(inp, CONTACT_PARAMS, N, "f32", face_cap=FACE_CAP)
+    o = oracle.contact(inp, CONTACT_PARAMS, N, "f32")
     g = run_gpu(inp, N, CONTACT_PARAMS, lanes=lanes)
     assert np.array_equal(g["collision"], o["collision"])
     assert (o["collision"] == 1).sum() > 300 and (o["collision"] == 0).sum() > 300
@@ -73,7 +71,7 @@ def test_bitexact_hull64_hist_stride4():
     p = dict(CONTACT_PARAMS, num_vertices_max=64)
     inp, N = make_pairs(800, seed=12, V=64, n_min=8, n_max=64)
     inp["hist"] = (np.random.default_rng(5).normal(size=inp["hist"].shape) * 1e-4).astype(np.float32)
-    o = oracle.contact(inp, p, N, "f32", hist_stride4=True, face_cap=FACE_CAP)
+    o = oracle.contact(inp, p, N, "f32", hist_stride4=True)
     g = run_gpu(inp, N, p, lanes=16, hist_mode=1)
     assert np.array_equal(g["collision"], o["collision"])
     assert bits_equal(g["diag"], o["diag"][:, :10])
@@ -86,7 +84,7 @@ def test_stride1_history_nonzero_input():
     # the reference reads displacement_tang[P..P+2] and writes [P..P+3] (overlapping rows)
     inp, N = make_pairs(400, seed=13)
     inp["hist"] = (np.random.default_rng(7).normal(size=inp["hist"].shape) * 1e-4).astype(np.float32)
-    o = oracle.contact(inp, CONTACT_PARAMS, N, "f32", face_cap=FACE_CAP)
+    o = oracle.contact(inp, CONTACT_PARAMS, N, "f32")
     g = run_gpu(inp, N, CONTACT_PARAMS)
     assert bits_equal(g["hist"], o["hist"])
     assert bits_equal(g["force"], o["force"])
@@ -96,7 +94,7 @@ def test_stride1_history_nonzero_input():
 def test_walls_and_shared_particles():
     p = dict(CONTACT_PARAMS, num_particles_wall=40, Kn_wall=3e4, en_wall=0.5, et_wall=0.6, mu_wall=0.3)
     inp, N = make_pairs(1200, seed=14, unique_ids=False, n_particles=200)
-    o = oracle.contact(inp, p, N, "f32", face_cap=FACE_CAP)
+    o = oracle.contact(inp, p, N, "f32")
     g = run_gpu(inp, N, p)
     assert np.array_equal(g["collision"], o["collision"])
     assert bits_equal(g["diag"], o["diag"][:, :10])
@@ -107,8 +105,8 @@ def test_walls_and_shared_particles():
 
 def test_against_fp64_oracle():
     inp, N = make_pairs(1500, seed=15)
-    o32 = oracle.contact(inp, CONTACT_PARAMS, N, "f32", face_cap=FACE_CAP)
-    o64 = oracle.contact(inp, CONTACT_PARAMS, N, "f64", face_cap=FACE_CAP)
+    o32 = oracle.contact(inp, CONTACT_PARAMS, N, "f32")
+    o64 = oracle.contact(inp, CONTACT_PARAMS, N, "f64")
     g = run_gpu(inp, N, CONTACT_PARAMS)
     # flags: identical except pairs whose FP64 separation/depth lies within 1e-9
     band = (o64["collision"] == 1) & (np.abs(o64["diag"][:, 0]) < 1e-9)
@@ -130,7 +128,7 @@ def test_cube_known_answer():
     # |F| = Kn * depth for a pair at rest (MWDiem's contact law, no damping term without motion)
     assert abs(np.linalg.norm(g["force"][0]) - 1e4 * 0.1) < 1e-2
     assert np.allclose(g["force"][0], -g["force"][1])
-    o = oracle.contact(inp, p, 2, "f32", face_cap=FACE_CAP)
+    o = oracle.contact(inp, p, 2, "f32")
     assert bits_equal(g["force"], o["force"])
 
 
@@ -144,7 +142,7 @@ def test_separated_and_degenerate():
     inp2["B_com"] = inp2["A_com"].copy()
     inp2["B_verts"] = inp2["A_verts"].copy()
     inp2["B_nv"] = inp2["A_nv"].copy()
-    o = oracle.contact(inp2, CONTACT_PARAMS, N2, "f32", face_cap=FACE_CAP)
+    o = oracle.contact(inp2, CONTACT_PARAMS, N2, "f32")
     g2 = run_gpu(inp2, N2, CONTACT_PARAMS)
     assert np.array_equal(g2["collision"], o["collision"])
     assert bits_equal(g2["diag"], o["diag"][:, :10])
@@ -160,7 +158,7 @@ def test_support_ties_first_index():
             n = int(nv[p])
             inp[k][p, n:2 * n] = inp[k][p, :n]
         nv *= 2
-    o = oracle.contact(inp, CONTACT_PARAMS, N, "f32", face_cap=FACE_CAP)
+    o = oracle.contact(inp, CONTACT_PARAMS, N, "f32")
     g = run_gpu(inp, N, CONTACT_PARAMS, lanes=8)
     assert np.array_equal(g["collision"], o["collision"])
     assert bits_equal(g["diag"], o["diag"][:, :10])
@@ -170,7 +168,7 @@ def test_empty_and_single():
     inp, N = make_pairs(1, seed=19)
     g = run_gpu(select(inp, slice(0, 0)), N, CONTACT_PARAMS)
     assert g["collision"].shape == (0,) and np.all(g["force"] == 0)
-    o = oracle.contact(inp, CONTACT_PARAMS, N, "f32", face_cap=FACE_CAP)
+    o = oracle.contact(inp, CONTACT_PARAMS, N, "f32")
     g1 = run_gpu(inp, N, CONTACT_PARAMS)
     assert np.array_equal(g1["collision"], o["collision"])
     assert bits_equal(g1["force"], o["force"])
@@ -189,6 +187,27 @@ def test_device_tensors_in_place():
         p["en_wall"], p["et_wall"], p["mu_wall"], p["num_particles_wall"], F, T, p["num_vertices_max"], d["qA"],
         d["qB"], p["timestep"], d["IsA"], d["IsB"])
     assert F2 is F and T2 is T and hist is d["hist"]
-    o = oracle.contact(inp, p, N, "f32", face_cap=FACE_CAP)
+    o = oracle.contact(inp, p, N, "f32")
     assert bits_equal(F.cpu().numpy(), o["force"])
     assert np.array_equal(coll.cpu().numpy(), o["collision"])
+
+
+@pytest.mark.parametrize("lanes", [8, 32])
+def test_epa_beyond_128_faces_resolves_like_the_oracle(lanes):
+    # a deep overlap of two 32-64-vertex hulls whose EPA creates 129 faces in all: an append-only face
+    # list of 128 entries stopped it with EPA_OVERFLOW; the compacted list holds only the live faces
+    # (at most 2 x 30 - 4 = 56 within the reference's iteration limit) and finishes it, as the oracle,
+    # which has no limit on faces created, does
+    inp, N = make_pairs(2000, seed=242, V=64, n_min=32, n_max=64, dist=(0.3, 1.2))
+    p = dict(CONTACT_PARAMS, num_vertices_max=64)
+    sub = select(inp, np.arange(1040, 1070))
+    o = oracle.contact(sub, p, N, "f32")
+    assert o["counters"][14, 9] == 129 and not o["status"][14] & oracle.ST_EPA_OVERFLOW
+    assert o["collision"][14] == 1
+    # with creation capped at 128 faces the same pair overflows
+    assert oracle.contact(sub, p, N, "f32", face_cap=128)["status"][14] & oracle.ST_EPA_OVERFLOW
+    g = run_gpu(sub, N, p, lanes=lanes)
+    assert not g["status"] & 2, "EPA_OVERFLOW"
+    assert np.array_equal(g["collision"], o["collision"])
+    assert bits_equal(g["diag"], o["diag"][:, :10])
+    assert bits_equal(g["force"], o["force"]) and bits_equal(g["torque"], o["torque"])

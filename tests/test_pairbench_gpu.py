@@ -32,7 +32,7 @@ def test_pairs_vs_oracle(two_pass, lanes):
     torch.cuda.synchronize()
     coll = ps.w["collision"].cpu().numpy()
     idx = np.arange(6000)
-    o = oracle.contact(ps.gather(idx), ps.params, 12000, "f32", face_cap=128)
+    o = oracle.contact(ps.gather(idx), ps.params, 12000, "f32")
     assert np.array_equal(coll, o["collision"])
     assert 0.3 < (coll == 1).mean() < 0.8
     F = ps.t["force"][:, :3].cpu().numpy()
@@ -58,5 +58,5 @@ def test_pairs_large_properties():
     # a sample still matches the oracle exactly
     rng = np.random.default_rng(0)
     idx = np.sort(rng.choice(n, size=3000, replace=False))
-    o = oracle.contact(ps.gather(idx), ps.params, 2 * n, "f32", face_cap=128)
+    o = oracle.contact(ps.gather(idx), ps.params, 2 * n, "f32")
     assert np.array_equal(coll[idx], o["collision"])

@@ -46,7 +46,7 @@ def test_pairs_flags_forces_step0():
     torch.cuda.synchronize()
     coll = sim.w["collision"][: len(pairs)].cpu().numpy()
     inp = stepper.gather_from_sim(sim, pairs, ref.V)
-    o = oracle.contact(inp, ref.params, sim.n, "f32", face_cap=128)
+    o = oracle.contact(inp, ref.params, sim.n, "f32")
     assert np.array_equal(coll, o["collision"])
     assert (coll == 1).sum() > 50
     W = sp.n_walls
@@ -282,7 +282,7 @@ def test_sphere_filter_drops_only_noncontacts():
     kept = oriented(pc)
     assert kept <= oriented(pf) and len(kept) < len(pf)
     ref = stepper.RefStepper(sp)
-    o = oracle.contact(stepper.gather_from_sim(full, pf, ref.V), ref.params, full.n, "f32", face_cap=128)
+    o = oracle.contact(stepper.gather_from_sim(full, pf, ref.V), ref.params, full.n, "f32")
     dropped = np.array([tuple(p) not in kept for p in pf.tolist()])
     assert np.all(o["collision"][dropped] == 0)
     assert np.all(o["counters"][dropped, 0] == 1)   # settled by the first support query
@@ -330,7 +330,7 @@ def test_deterministic_sums_equal_serial_loop(lanes):
     sim.narrow_force()
     torch.cuda.synchronize()
     ref = stepper.RefStepper(sp)
-    o = oracle.contact(stepper.gather_from_sim(sim, pairs, ref.V), ref.params, sim.n, "f32", face_cap=128)
+    o = oracle.contact(stepper.gather_from_sim(sim, pairs, ref.V), ref.params, sim.n, "f32")
     coll = sim.w["collision"][: len(pairs)].cpu().numpy()
     assert np.array_equal(coll, o["collision"]) and (coll == 1).sum() > 100
     W = sp.n_walls
@@ -411,7 +411,7 @@ def test_persistent_history_matches_oracle_over_steps(lanes):
                 hist[k, :3] = v if a < b else -v
                 reused += 1
         inp["hist"] = hist
-        o = oracle.contact(inp, ref.params, sim.n, "f32", hist_stride4=True, face_cap=128)
+        o = oracle.contact(inp, ref.params, sim.n, "f32", hist_stride4=True)
         sim.narrow_force()
         torch.cuda.synchronize()
         coll = sim.w["collision"][: len(pairs)].cpu().numpy()
@@ -444,7 +444,7 @@ def test_physical_law_sums_equal_oracle():
     sim.narrow_force()
     torch.cuda.synchronize()
     ref = stepper.RefStepper(sp)
-    o = oracle.contact(stepper.gather_from_sim(sim, pairs, ref.V), ref.params, sim.n, "f32", face_cap=128,
+    o = oracle.contact(stepper.gather_from_sim(sim, pairs, ref.V), ref.params, sim.n, "f32",
                        inv_mass=stepper.inv_mass_from_sim(sim, pairs))
     coll = sim.w["collision"][: len(pairs)].cpu().numpy()
     assert np.array_equal(coll, o["collision"]) and (coll == 1).sum() > 100
@@ -533,3 +533,39 @@ def test_inlet_rows_enter_on_schedule():
     torch.cuda.synchronize()
     assert np.array_equal(graph.active_rows().cpu().numpy(), act)
     assert np.abs(graph.t["pos"].cpu().numpy()[act] - pos[act]).max() <= 1e-6 * 16.0
+
+
+def test_inlet_run_matches_reference_path():
+    # the inlet's physics, not only its schedule: the reference path (oracle/stepper.py) runs the same
+    # activation schedule with the same spawn points (MWDiem.py:685-714), and the 30-step run of the
+    # device step must stay within the short-horizon bars of the reference path, rows entering
+    # (some of them overlapping on arrival) included
+    from mwdiem_gb300.sim import InletSpec, Simulator
+    sp = dense_scene(n=300, seed=31, vel=0.0)
+    inl = InletSpec(period=5, per_spawn=2, initial=200, lo=(-5.0, -5.0, 15.5), hi=(5.0, 5.0, 17.5), seed=1)
+    W = sp.n_walls
+    sim = Simulator(sp, inlet=inl, collect_collisions=True)
+    spawn = sim.inlet_t["spawn_pos"][:, :3].cpu().numpy()
+    ref = stepper.RefStepper(sp, inlet=(inl.period, inl.per_spawn, W + inl.initial, spawn))
+    steps = 30
+    for _ in range(steps):
+        ref.step()
+    sim.step(steps)
+    torch.cuda.synchronize()
+    act = sim.active_rows().cpu().numpy()
+    assert int(act.sum()) == ref.active_end == W + 200 + 2 * 6
+    rows = np.nonzero(act)[0]
+    rows = rows[rows >= W]
+    g = sim.reference_state()
+    dpos = np.abs(g["com"][rows] - ref.st["com"][rows]).max()
+    vmax = np.abs(ref.st["v"][rows]).max()
+    dvel = np.abs(g["v"][rows] - ref.st["v"][rows]).max()
+    dq = np.abs(g["q"][rows] - ref.st["q"][rows]).max()
+    entered = np.arange(W + 200, W + 212)
+    moved = np.abs(ref.st["v"][entered]).max()
+    print(f"inlet, {steps} steps: |dpos| {dpos:.3e} |dv| {dvel:.3e} (vmax {vmax:.3e}) |dq| {dq:.3e}; "
+          f"entered rows' largest speed {moved:.3e}")
+    assert dpos <= 2e-6 * 16.0
+    assert dvel <= 1e-3 * vmax
+    assert dq <= 1e-4
+    sim.check_status()
