@@ -48,7 +48,7 @@ enum {
 };
 
 #define MWD_EPA_FACE_CAP 128   /* live EPA faces per pair (the list is compacted as faces are deleted) */
-#define MWD_EPA_COUNT_INTS 8   /* ints of mwd_work.epa_count */
+#define MWD_EPA_COUNT_INTS 256 /* ints of mwd_work.epa_count */
 #define MWD_EPA_VERT_CAP 32    /* EPA polytope vertices per pair (4 + 25 iterations + 1) */
 #define MWD_HULL_CAP 64        /* hull vertices per side staged in shared memory */
 #define MWD_CELL_CAP 306       /* members per cell handled by the CPython set-order emulation */
@@ -291,8 +291,9 @@ typedef struct {
     uint64_t* work_counters; /* optional (3,), added to by the narrow phase: vertex dot products of the
                               support queries, EPA faces created, support queries (NULL: not counted) */
     int32_t* epa_count;    /* (MWD_EPA_COUNT_INTS,) 8-byte aligned, two-pass narrow phase: [0] pairs found in
-                              contact by the GJK pass, [2..3] the EPA pass's work queue (uint64), the
-                              rest reserved; zeroed by the broad phase of mwd_step, or by
+                              contact by the GJK pass, [2..3] the EPA pass's work queue (uint64), [4] and
+                              [8..] the records whose EPA face list overflowed (run again after the
+                              pass); [0..7] are zeroed by the broad phase of mwd_step, or by
                               mwd_narrow_force when it runs alone */
     void* epa_rec;         /* (epa_cap, 80 B): their simplex; NULL selects the single-pass kernel */
     int64_t epa_cap;

@@ -30,7 +30,7 @@ ST_FLY_RESET = 512
 ST_HIST_OVERFLOW = 1024
 
 EPA_FACE_CAP = 128
-EPA_COUNT_INTS = 8    # ints of mwd_work.epa_count: the EPA record count and the EPA pass's 64-bit work queue
+EPA_COUNT_INTS = 256  # ints of mwd_work.epa_count: EPA record count, work queue, overflow retry list
 EPA_VERT_CAP = 32
 HULL_CAP = 64
 CELL_CAP = 306

@@ -289,32 +289,6 @@ __device__ bool pyset_order(const int* m, int k, int* out, int* tab, unsigned ch
     return true;
 }
 
-// list(set) of up to 4 members m[0..k) (ascending ids, inserted in that order), in registers: CPython's
-// table stays at 8 slots below 5 entries (it grows when fill * 5 >= mask * 3 = 21), and with mask 7
-// the linear probes never run (they need i + 9 <= mask), so each member lands at hash & 7 or, while
-// that slot is taken, at the perturbation sequence i = 5 i + 1 + (perturb >>= 5) (mod 8); the list is
-// the members in slot order.  The same result as pyset_order for these k.
-__device__ __forceinline__ void pyset_order4(const int* m, int k, int* out, int base)
-{
-    unsigned used = 0;
-    int slot[4];
-    for (int e = 0; e < k; ++e) {
-        const uint64_t h = (uint64_t)(uint32_t)(m[e] - base);
-        unsigned i = (unsigned)(h & 7u);
-        uint64_t perturb = h;
-        while (used & (1u << i)) {
-            perturb >>= 5;
-            i = (unsigned)((i * 5ull + 1ull + perturb) & 7u);
-        }
-        used |= 1u << i;
-        slot[e] = (int)i;
-    }
-    int c = 0;
-    for (int sidx = 0; sidx < 8; ++sidx)
-        for (int e = 0; e < k; ++e)
-            if (slot[e] == sidx) out[c++] = m[e];
-}
-
 // cells up to SMALL_CELL members are ordered by one thread with the table in local memory; larger
 // cells go to a list handled by one warp each with the table in shared memory
 constexpr int SMALL_CELL = 32;
@@ -371,8 +345,8 @@ __global__ void assign_kernel(BroadArgs a)
     pdl_launch_dependents();
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (a.append) *a.n_pairs = 0;  // appended to by pairs_append_kernel
-        if (a.epa_count)  // the EPA record count and the EPA pass's work queue
-            for (int k = 0; k < MWD_EPA_COUNT_INTS; ++k) a.epa_count[k] = 0;
+        if (a.epa_count)  // the EPA record count, the EPA pass's work queue and retry count
+            for (int k = 0; k < 8; ++k) a.epa_count[k] = 0;
     }
     const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= a.row_hi) return;
@@ -449,23 +423,6 @@ __device__ __forceinline__ int order_row(const BroadArgs& a, int r)
     for (int j = s; j < e; ++j)
         if (a.scatter_out[j] < r) return -1;  // the smallest id of the cell orders it
     if (k > SMALL_CELL) return g;
-    const int base = a.info ? a.scenes[scene_of(a, r)].row_begin : 0;
-    if (k <= 4) {
-        // a few members: sorted and ordered in registers
-        int m4[4], o4[4];
-        for (int j = 0; j < k; ++j) {
-            const int v = a.scatter_out[s + j];
-            int i = j;
-            while (i > 0 && m4[i - 1] > v) {
-                m4[i] = m4[i - 1];
-                --i;
-            }
-            m4[i] = v;
-        }
-        pyset_order4(m4, k, o4, base);
-        for (int j = 0; j < k; ++j) place(a, s + j, o4[j], g);
-        return -1;
-    }
     int m[SMALL_CELL];
     for (int j = 0; j < k; ++j) {
         int v = a.scatter_out[s + j];
@@ -479,6 +436,7 @@ __device__ __forceinline__ int order_row(const BroadArgs& a, int r)
     int o[SMALL_CELL];
     int tab[SMALL_TAB], tmp[SMALL_TAB];
     unsigned char used[SMALL_TAB], used2[SMALL_TAB];
+    const int base = a.info ? a.scenes[scene_of(a, r)].row_begin : 0;
     pyset_order<SMALL_TAB>(m, k, o, tab, used, tmp, used2, base);
     for (int j = 0; j < k; ++j) place(a, s + j, o[j], g);
     return -1;

@@ -14,12 +14,12 @@
 //    desc, index asc), which reproduces the reference's strict-'>' first-index tie break;
 //  * the simplex logic runs redundantly (identically) on every lane of the group, so control flow
 //    stays group-uniform;
-//  * EPA keeps a face list of MWD_EPA_FACE_CAP entries in shared memory, append-only like the
-//    reference's T[50]/n[50]/dist[50] (which overflow past 50 faces) until it would overflow, when it
-//    is compacted (deleted faces removed in order); the face scan, the visibility test, the horizon
-//    edge count (the reference's 50x50 delpair matrix, replaced by counting over the deleted-face
-//    list) and the new faces are computed lane-parallel, with ballots to keep the reference's face
-//    order;
+//  * EPA keeps an append-only face list of MWD_EPA_FACE_CAP faces in shared memory, like the
+//    reference's T[50]/n[50]/dist[50] (which overflow past 50 faces); a pair that outgrows it runs
+//    again with the deleted faces removed from the list (epa_compacting); the face scan, the
+//    visibility test, the horizon edge count (the reference's 50x50 delpair matrix, replaced by
+//    counting over the deleted-face list) and the new faces are computed lane-parallel, with ballots
+//    to keep the reference's face order;
 //  * force/torque are accumulated with float atomics (skipped for wall rows in table mode, whose
 //    forces the reference discards, MWDiem.py:977-978).
 #include <float.h>
@@ -34,22 +34,13 @@ namespace {
 constexpr int FCAP = MWD_EPA_FACE_CAP;
 constexpr int VCAP = MWD_EPA_VERT_CAP;
 
-// per-group shared memory (the hull staging area follows, 2 * hull_cap float4).  Like the reference's
-// arrays, the face list keeps deleted faces in place with distance 3e20 (.cu:541-542) and appends new
-// ones.  When it would overflow, it is compacted instead: the deleted faces leave it, keeping the
-// order of the rest, and the earliest created of them -- the only one the minimum search could still
-// choose -- is kept aside (dn, dt), with every face's creation index (fc) for the search's ties.
+// per-group shared memory (the hull staging area follows, 2 * hull_cap float4)
 struct EpaMem {
     float4 fn[FCAP];       // face normal xyz, distance
     uint32_t ft[FCAP];     // T0 | T1 << 8 | T2 << 16 | (valid + 2) << 24
-    uint16_t fc[FCAP];     // creation index of each face (its index in the reference's arrays)
     float4 pv[VCAP];       // polytope vertices
     uint16_t pab[VCAP];    // support index on A | on B << 8
     uint32_t del[FCAP];    // faces deleted in this iteration, in index order: vertices T0 T1 T2 | face << 24
-    float4 dn;             // the earliest-created face a compaction removed: normal, distance 3e20
-    uint32_t dt;           // its vertices (ft layout)
-    float4 cn;             // the face chosen in the iteration a compaction happened in, and
-    uint32_t ct;           // its vertices (ft layout)
 };
 
 __device__ __forceinline__ int ft_v(uint32_t t, int k) { return (t >> (8 * k)) & 0xff; }
@@ -100,6 +91,12 @@ __device__ __forceinline__ unsigned long long* epa_queue(const NarrowArgs& a)
 {
     return reinterpret_cast<unsigned long long*>(a.epa_count + 2);
 }
+
+// EPA records whose face list overflowed, run again by epa_retry_kernel after the EPA pass: their
+// count at int [4] of the block epa_count points to, the record indices from int [8]
+constexpr int EPA_RETRY_CAP = MWD_EPA_COUNT_INTS - 8;
+__device__ __forceinline__ int* epa_retry_count(const NarrowArgs& a) { return a.epa_count + 4; }
+__device__ __forceinline__ int32_t* epa_retry_list(const NarrowArgs& a) { return a.epa_count + 8; }
 
 // The next `amount` items of a queue for the calling group: its first lane takes them with one atomic.
 template <int LPP>
@@ -280,15 +277,17 @@ __device__ __forceinline__ bool epa_converged(float x, float p)
     return (double)x * 1.00001 > (double)p && (double)x * 0.99999 < (double)p;
 }
 
-// AddTriangle (.cu:270-325), one face per calling lane
-__device__ __forceinline__ void add_face(EpaMem& m, int e0, int e1, int e2, int f)
+// AddTriangle (.cu:270-325): normal and distance of the face (e0, e1, e2), its winding (t1, t2) and
+// validity (1, or -2 with distance 1e30 when the origin's projection falls outside it)
+__device__ __forceinline__ float4 face_geom(const EpaMem& m, int e0, int e1, int e2, int& t1, int& t2, int& valid)
 {
     f3 a = xyz(m.pv[e0]), b = xyz(m.pv[e1]), c = xyz(m.pv[e2]);
     f3 n = cross(b - a, c - b);
     float len = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
     n = n / len;
     float dist = dot(n, a);
-    int t1 = e1, t2 = e2;
+    t1 = e1;
+    t2 = e2;
     if (dist < 0.f) {
         t2 = e1;
         t1 = e2;
@@ -300,12 +299,19 @@ __device__ __forceinline__ void add_face(EpaMem& m, int e0, int e1, int e2, int 
     if (dot(cross(B - A, n), A * (-1.f)) < 0.f)
         if (dot(cross(C - B, n), B * (-1.f)) < 0.f)
             if (dot(cross(A - C, n), C * (-1.f)) < 0.f) inside = true;
-    int valid = 1;
+    valid = 1;
     if (!inside) {
         valid = -2;
         dist = 1e30f;
     }
-    m.fn[f] = f4(n, dist);
+    return f4(n, dist);
+}
+
+// AddTriangle into slot f of the face list, one face per calling lane
+__device__ __forceinline__ void add_face(EpaMem& m, int e0, int e1, int e2, int f)
+{
+    int t1, t2, valid;
+    m.fn[f] = face_geom(m, e0, e1, e2, t1, t2, valid);
     m.ft[f] = ft_make(e0, t1, t2, valid);
 }
 
@@ -324,65 +330,14 @@ struct EpaResult {
     uint32_t status;
 };
 
-// Removes the deleted faces (valid 0, and -1 for those of this iteration) from the face list, keeping
-// the order of the others; the earliest created of the removed faces replaces the one kept aside when
-// it was created earlier (del_c: that face's creation index, uniform over the group).  Returns the
-// number of faces left.
-template <int LPP>
-__device__ __noinline__ int epa_compact(const Group<LPP>& g, EpaMem& m, int nt, uint32_t& del_c)
-{
-    const int lane0 = (int)(threadIdx.x & 31) - g.lane;
-    int nk = 0;
-    bool first = true;
-    for (int base = 0; base < nt; base += LPP) {
-        const int f = base + g.lane;
-        bool gone = false, keep = false;
-        float4 fv = make_float4(0.f, 0.f, 0.f, 0.f);
-        uint32_t t = 0;
-        uint16_t c = 0;
-        if (f < nt) {
-            fv = m.fn[f];
-            t = m.ft[f];
-            c = m.fc[f];
-            const int vl = ft_valid(t);
-            gone = vl == 0 || vl == -1;
-            keep = !gone;
-        }
-        const unsigned bg = g.ballot(gone), bk = g.ballot(keep);
-        g.sync();
-        if (bg && first) {
-            // the first removed face in list (= creation) order
-            const int fl = __ffs(bg) - 1;
-            const uint32_t c0 = (uint32_t)__shfl_sync(g.mask, (int)c, lane0 + fl);
-            if (c0 < del_c) {
-                if (g.lane == fl) {
-                    m.dn = make_float4(fv.x, fv.y, fv.z, 3e20f);
-                    m.dt = (t & 0x00ffffffu) | ((uint32_t)(0 + 2) << 24);
-                }
-                del_c = c0;
-            }
-            first = false;
-        }
-        if (keep) {
-            const int o = nk + __popc(bk & g.lt_mask());
-            if (o != f) {
-                m.fn[o] = fv;
-                m.ft[o] = t;
-                m.fc[o] = c;
-            }
-        }
-        nk += __popc(bk);
-    }
-    g.sync();
-    return nk;
-}
-
+// EPA (.cu:328-603) with the reference's append-only face list: deleted faces stay in it at distance
+// 3e20 (.cu:541-542).  A pair whose list would outgrow FCAP stops with MWD_ST_EPA_OVERFLOW and is run
+// again by epa_compacting.
 template <int LPP>
 __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, const float4* hB, int nB,
                     f3 S1, int a1, int b1, f3 S2, int a2, int b2, f3 S3, int a3, int b3, f3 S4, int a4, int b4,
                     EpaResult& r, Work3& wk)
 {
-    constexpr uint32_t NONE = 0xffffffffu;
     r.status = 0;
     g.sync();
     if (g.lane == 0) {
@@ -395,21 +350,15 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
         // faces (0,1,2), (1,2,3), (2,0,3), (0,1,3), packed as 4-bit vertex numbers (no local array)
         const unsigned long long e = 0x310302321210ull >> (12 * g.lane);
         add_face(m, (int)(e & 0xf), (int)((e >> 4) & 0xf), (int)((e >> 8) & 0xf), g.lane);
-        m.fc[g.lane] = (uint16_t)g.lane;
     }
     g.sync();
     wk.faces += 4;
-    int nt = 4, nv = 4, counter = 0;
-    // indmin: the face chosen (>= 0: list index; -1: the face kept aside, m.dn; -2: the chosen face
-    // saved before a compaction, m.cn)
-    int indmin = 0;
-    uint32_t created = 4;
-    uint32_t del_c = NONE;  // creation index of the face in m.dn (NONE: no compaction yet)
+    int nt = 4, nv = 4, counter = 0, indmin = 0;
     float xmin_old = 1e29f;
     float proj = 2 * xmin_old + 1;
     float xmin_new = 0.f;
     while (xmin_old < proj) {
-        // array_min_finder (.cu:41-53): first index of the minimum distance over every face created
+        // first index of the minimum distance
         float bv = __int_as_float(0x7fffffff);
         int bi = 0x7fffffff;
         for (int f = g.lane; f < nt; f += LPP) {
@@ -422,23 +371,9 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
             const unsigned km = __reduce_min_sync(g.mask, k);
             bi = (int)__reduce_min_sync(g.mask, k == km ? (unsigned)bi : 0xffffffffu);
         }
-        if (del_c == NONE) {
-            // the search starts from face 0's distance: a NaN there keeps face 0
-            float d0 = m.fn[0].w;
-            indmin = (d0 != d0) ? 0 : bi;
-        } else {
-            // after a compaction the faces it removed (all at 3e20) are represented by the earliest
-            // created of them: it wins when no listed face is closer, or an equally close one was
-            // created later; face 0 is at the head of the list as long as it has not been removed
-            indmin = bi;
-            if (bi == 0x7fffffff) indmin = -1;
-            else {
-                const float lv = m.fn[bi].w;
-                if (lv > 3e20f || (lv == 3e20f && del_c < (uint32_t)m.fc[bi])) indmin = -1;
-            }
-            if (m.fc[0] == 0 && m.fn[0].w != m.fn[0].w) indmin = 0;
-        }
-        const float4 fm = indmin >= 0 ? m.fn[indmin] : m.dn;
+        float d0 = m.fn[0].w;
+        indmin = (d0 != d0) ? 0 : bi;
+        float4 fm = m.fn[indmin];
         xmin_new = fm.w;
         xmin_old = xmin_new;
         f3 n = xyz(fm);
@@ -475,27 +410,241 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
             ndel += __popc(b);
         }
         g.sync();
-        // the new faces (at most three per deleted face) might not fit: compact the list first
-        const bool compacted = nt + 3 * ndel > FCAP;
-        if (compacted) {
-            if (indmin >= 0) {
-                if (g.lane == 0) {
-                    m.cn = m.fn[indmin];
-                    m.ct = m.ft[indmin];
-                }
-                indmin = -2;
-            } else if (indmin == -1) {
-                if (g.lane == 0) {
-                    m.cn = m.dn;
-                    m.ct = m.dt;
-                }
-                indmin = -2;
-            }
-            g.sync();
-            nt = epa_compact<LPP>(g, m, nt, del_c);
-        }
         // horizon edges of the deleted faces, in face order then edge order (0,1),(1,2),(2,0);
         // an edge is kept when fewer than two delpair increments land on it (.cu:482-544)
+        int nnew = 0;
+        bool overflow = false;
+        for (int base = 0; base < 3 * ndel; base += LPP) {
+            int c = base + g.lane;
+            bool keep = false;
+            int e0 = 0, e1 = 0;
+            if (c < 3 * ndel) {
+                uint32_t t = m.del[c / 3];
+                int k = c % 3;
+                e0 = ft_v(t, k);
+                e1 = ft_v(t, k == 2 ? 0 : k + 1);
+                int cnt = 0;
+                for (int j = 0; j < ndel; ++j) {
+                    uint32_t u = m.del[j];
+                    int x = ft_v(u, 0), y = ft_v(u, 1), z = ft_v(u, 2);
+                    cnt += (e0 == y && e1 == x) + (e0 == x && e1 == y) + (e0 == z && e1 == y) +
+                           (e0 == y && e1 == z) + (e0 == x && e1 == z) + (e0 == z && e1 == x);
+                }
+                keep = cnt < 2;
+            }
+            unsigned b = g.ballot(keep);
+            if (keep) {
+                int f = nt + nnew + __popc(b & g.lt_mask());
+                if (f < FCAP) add_face(m, e0, e1, nv - 1, f);
+            }
+            nnew += __popc(b);
+        }
+        if (nt + nnew > FCAP) overflow = true;
+        g.sync();
+        for (int k = g.lane; k < ndel; k += LPP) {
+            int f = (int)(m.del[k] >> 24);
+            m.ft[f] = (m.ft[f] & 0x00ffffffu) | ((uint32_t)(0 + 2) << 24);
+            m.fn[f].w = 3e20f;
+        }
+        g.sync();
+        if (overflow) { r.status |= MWD_ST_EPA_OVERFLOW; break; }
+        nt += nnew;
+        wk.faces += (uint32_t)nnew;
+        counter = counter + 1;
+    }
+    g.sync();
+    r.depth = xmin_new;
+    // the contact point and everything after it (the force) are needed by one lane only: the others
+    // skip them, which keeps their FP64 operations (below and in contact_force) off the FP64 pipe
+    if (g.lane != 0) return;
+    uint32_t t = m.ft[indmin];
+    int a = ft_v(t, 0), b = ft_v(t, 1), c = ft_v(t, 2);
+    f3 n = xyz(m.fn[indmin]);
+    f3 Pr = n * r.depth;
+    f3 Va = xyz(m.pv[a]), Vb = xyz(m.pv[b]), Vc = xyz(m.pv[c]);
+    f3 v0 = Vb - Va, v1 = Vc - Va, v2 = Pr - Va;
+    if (dot(cross(v0, v1), n) < 0.f) {
+        v0 = Vc - Va;
+        v1 = Vb - Va;
+    }
+    float v00 = dot(v0, v0), v01 = dot(v0, v1), v11 = dot(v1, v1), v20 = dot(v2, v0), v21 = dot(v2, v1);
+    float den = v00 * v11 - v01 * v01;
+    float bv = (v11 * v20 - v01 * v21) / den;
+    float bw = (v00 * v21 - v01 * v20) / den;
+    float bu = (float)(1.0 - (double)bw - (double)bv);
+    int pa = m.pab[a], pb = m.pab[b], pc = m.pab[c];
+    r.fa[0] = pa & 0xff; r.fa[1] = pb & 0xff; r.fa[2] = pc & 0xff;
+    r.fb[0] = pa >> 8; r.fb[1] = pb >> 8; r.fb[2] = pc >> 8;
+    r.cpA = (xyz(hA[r.fa[0]]) * bu + xyz(hA[r.fa[1]]) * bv) + xyz(hA[r.fa[2]]) * bw;
+    r.cpB = (xyz(hB[r.fb[0]]) * bu + xyz(hB[r.fb[1]]) * bv) + xyz(hB[r.fb[2]]) * bw;
+    r.n = n;
+}
+
+// The EPA of a pair whose face list outgrew FCAP, run again from the same simplex: the same decisions
+// and arithmetic with the deleted faces removed from the list (the survivors keep their order) instead
+// of kept at 3e20.  Of the removed faces only the earliest created can still win the minimum search
+// (.cu:41-53: all are at 3e20, the first index wins): it is kept in the list's last slot, FCAP - 1, with
+// every face's creation index (its index in the reference's arrays) packed into its vertex word:
+// T0 | T1 << 5 | T2 << 10 | (valid + 2) << 15 | creation << 17.  At most 2 * 30 - 4 = 56 faces are
+// alive within the reference's iteration limit, so this list does not overflow.  Rarely needed: the
+// two-pass narrow phase runs the records that overflowed again in a kernel of their own after its EPA
+// pass, the single-pass kernel calls it out of line right after the overflow (epa_run).
+__device__ __forceinline__ int fc_v(uint32_t t, int k) { return (t >> (5 * k)) & 31; }
+__device__ __forceinline__ uint32_t fc_created(uint32_t t) { return t >> 17; }
+__device__ __forceinline__ uint32_t fc_make(int a, int b, int c, int valid, uint32_t created)
+{
+    return (uint32_t)a | ((uint32_t)b << 5) | ((uint32_t)c << 10) | ((uint32_t)(valid + 2) << 15) | (created << 17);
+}
+
+// contact points of the final face (.cu:548-600): barycentric coordinates of n * depth on the face
+// (winding swapped when its normal points the other way), applied to the support vertices of A and B
+__device__ __forceinline__ void epa_contact(const EpaMem& m, const float4* hA, const float4* hB, f3 n, int a, int b,
+                                            int c, EpaResult& r)
+{
+    f3 Pr = n * r.depth;
+    f3 Va = xyz(m.pv[a]), Vb = xyz(m.pv[b]), Vc = xyz(m.pv[c]);
+    f3 v0 = Vb - Va, v1 = Vc - Va, v2 = Pr - Va;
+    if (dot(cross(v0, v1), n) < 0.f) {
+        v0 = Vc - Va;
+        v1 = Vb - Va;
+    }
+    float v00 = dot(v0, v0), v01 = dot(v0, v1), v11 = dot(v1, v1), v20 = dot(v2, v0), v21 = dot(v2, v1);
+    float den = v00 * v11 - v01 * v01;
+    float bv = (v11 * v20 - v01 * v21) / den;
+    float bw = (v00 * v21 - v01 * v20) / den;
+    float bu = (float)(1.0 - (double)bw - (double)bv);
+    int pa = m.pab[a], pb = m.pab[b], pc = m.pab[c];
+    r.fa[0] = pa & 0xff; r.fa[1] = pb & 0xff; r.fa[2] = pc & 0xff;
+    r.fb[0] = pa >> 8; r.fb[1] = pb >> 8; r.fb[2] = pc >> 8;
+    r.cpA = (xyz(hA[r.fa[0]]) * bu + xyz(hA[r.fa[1]]) * bv) + xyz(hA[r.fa[2]]) * bw;
+    r.cpB = (xyz(hB[r.fb[0]]) * bu + xyz(hB[r.fb[1]]) * bv) + xyz(hB[r.fb[2]]) * bw;
+    r.n = n;
+}
+
+template <int LPP>
+__device__ __forceinline__ EpaResult epa_compacting(const Group<LPP>& g, EpaMem* mp, const float4* hA, int nA,
+                                                    const float4* hB, int nB, f3 S1, int a1, int b1, f3 S2, int a2,
+                                                    int b2, f3 S3, int a3, int b3, f3 S4, int a4, int b4, Work3* wkp)
+{
+    constexpr int SLOT = FCAP - 1;   // the earliest-created removed face
+    constexpr int LIVE = FCAP - 1;   // capacity of the live list
+    constexpr uint32_t NONE = 0xffffffffu;
+    EpaMem& m = *mp;
+    Work3 wk = *wkp;
+    EpaResult r;
+    r.status = 0;
+    g.sync();
+    if (g.lane == 0) {
+        m.pv[0] = f4(S1, 0.f); m.pv[1] = f4(S2, 0.f); m.pv[2] = f4(S3, 0.f); m.pv[3] = f4(S4, 0.f);
+        m.pab[0] = (uint16_t)(a1 | (b1 << 8)); m.pab[1] = (uint16_t)(a2 | (b2 << 8));
+        m.pab[2] = (uint16_t)(a3 | (b3 << 8)); m.pab[3] = (uint16_t)(a4 | (b4 << 8));
+    }
+    g.sync();
+    if (g.lane < 4) {
+        const unsigned long long e = 0x310302321210ull >> (12 * g.lane);
+        const int e0 = (int)(e & 0xf), e1 = (int)((e >> 4) & 0xf), e2 = (int)((e >> 8) & 0xf);
+        int t1, t2, valid;
+        m.fn[g.lane] = face_geom(m, e0, e1, e2, t1, t2, valid);
+        m.ft[g.lane] = fc_make(e0, t1, t2, valid, (uint32_t)g.lane);
+    }
+    g.sync();
+    wk.faces += 4;
+    int nt = 4, nv = 4, counter = 0;
+    uint32_t created = 4;
+    uint32_t del_c = NONE;  // creation index of the face in the slot (NONE: none removed yet)
+    const int lane0 = (int)(threadIdx.x & 31) - g.lane;
+    float xmin_old = 1e29f;
+    float proj = 2 * xmin_old + 1;
+    float xmin_new = 0.f;
+    float4 fm = make_float4(0.f, 0.f, 0.f, 0.f);  // the face chosen last, and its vertex word
+    uint32_t tm = 0;
+    while (xmin_old < proj) {
+        float bv = __int_as_float(0x7fffffff);
+        int bi = 0x7fffffff;
+        for (int f = g.lane; f < nt; f += LPP) {
+            float v = m.fn[f].w;
+            if (min_better(v, f, bv, bi)) { bv = v; bi = f; }
+        }
+        {
+            const unsigned k = (bv != bv) ? 0xffffffffu : fkey(bv);
+            const unsigned km = __reduce_min_sync(g.mask, k);
+            bi = (int)__reduce_min_sync(g.mask, k == km ? (unsigned)bi : 0xffffffffu);
+        }
+        // the removed faces (all at 3e20) are represented by the earliest created of them
+        bool use_slot = false;
+        if (del_c != NONE) {
+            if (bi == 0x7fffffff) use_slot = true;
+            else {
+                const float lv = m.fn[bi].w;
+                use_slot = lv > 3e20f || (lv == 3e20f && del_c < fc_created(m.ft[bi]));
+            }
+        }
+        // the search starts from face 0's distance: a NaN there keeps face 0
+        if (nt > 0 && fc_created(m.ft[0]) == 0 && m.fn[0].w != m.fn[0].w) {
+            use_slot = false;
+            bi = 0;
+        }
+        fm = use_slot ? m.fn[SLOT] : m.fn[bi];
+        tm = use_slot ? m.ft[SLOT] : m.ft[bi];
+        xmin_new = fm.w;
+        xmin_old = xmin_new;
+        f3 n = xyz(fm);
+        f3 s;
+        int sa, sb;
+        support<LPP>(g, hA, nA, hB, nB, n, s, sa, sb, wk);
+        proj = dot(n, s);
+        if (xmin_old > proj || epa_converged(xmin_old, proj)) break;
+        if (counter > 49) { r.status |= MWD_ST_EPA_NOCONV; break; }
+        counter = counter + 1;
+        if (nv >= VCAP) { r.status |= MWD_ST_EPA_OVERFLOW; break; }
+        g.sync();
+        if (g.lane == 0) {
+            m.pv[nv] = f4(s, 0.f);
+            m.pab[nv] = (uint16_t)(sa | (sb << 8));
+        }
+        nv++;
+        // faces the new vertex sees are deleted, collected in list order; the others move down
+        int ndel = 0, nkeep = 0;
+        for (int base = 0; base < nt; base += LPP) {
+            const int f = base + g.lane;
+            bool dead = false, live = false;
+            float4 fv = make_float4(0.f, 0.f, 0.f, 0.f);
+            uint32_t t = 0;
+            if (f < nt) {
+                fv = m.fn[f];
+                t = m.ft[f];
+                dead = dot(s - xyz(m.pv[fc_v(t, 0)]), xyz(fv)) >= 0.f;
+                live = !dead;
+            }
+            const unsigned bd = g.ballot(dead), bl = g.ballot(live);
+            g.sync();
+            if (dead)
+                m.del[ndel + __popc(bd & g.lt_mask())] = (uint32_t)fc_v(t, 0) | ((uint32_t)fc_v(t, 1) << 8) |
+                                                         ((uint32_t)fc_v(t, 2) << 16);
+            if (live) {
+                const int o = nkeep + __popc(bl & g.lt_mask());
+                if (o != f) {
+                    m.fn[o] = fv;
+                    m.ft[o] = t;
+                }
+            }
+            if (bd && ndel == 0) {
+                // the first face deleted in this iteration is the earliest created of them
+                const int fl = __ffs(bd) - 1;
+                const uint32_t c0 = (uint32_t)__shfl_sync(g.mask, (int)fc_created(t), lane0 + fl);
+                if (c0 < del_c) {
+                    if (g.lane == fl) {
+                        m.fn[SLOT] = make_float4(fv.x, fv.y, fv.z, 3e20f);
+                        m.ft[SLOT] = (t & ~((uint32_t)3 << 15)) | ((uint32_t)(0 + 2) << 15);
+                    }
+                    del_c = c0;
+                }
+            }
+            ndel += __popc(bd);
+            nkeep += __popc(bl);
+        }
+        g.sync();
+        // horizon edges, as in epa (.cu:482-544); the new faces follow the survivors
         int nnew = 0;
         for (int base = 0; base < 3 * ndel; base += LPP) {
             int c = base + g.lane;
@@ -518,57 +667,50 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
             unsigned b = g.ballot(keep);
             if (keep) {
                 const int q = nnew + __popc(b & g.lt_mask());
-                const int f = nt + q;
-                if (f < FCAP) {
-                    add_face(m, e0, e1, nv - 1, f);
-                    m.fc[f] = (uint16_t)(created + (uint32_t)q);
+                const int f = nkeep + q;
+                if (f < LIVE) {
+                    int t1, t2, valid;
+                    m.fn[f] = face_geom(m, e0, e1, nv - 1, t1, t2, valid);
+                    m.ft[f] = fc_make(e0, t1, t2, valid, created + (uint32_t)q);
                 }
             }
             nnew += __popc(b);
         }
         g.sync();
-        if (!compacted) {
-            // the deleted faces stay in the list (.cu:539-542)
-            for (int k = g.lane; k < ndel; k += LPP) {
-                int f = (int)(m.del[k] >> 24);
-                m.ft[f] = (m.ft[f] & 0x00ffffffu) | ((uint32_t)(0 + 2) << 24);
-                m.fn[f].w = 3e20f;
-            }
-            g.sync();
-        }
-        if (nt + nnew > FCAP) { r.status |= MWD_ST_EPA_OVERFLOW; break; }
-        nt += nnew;
+        if (nkeep + nnew > LIVE) { r.status |= MWD_ST_EPA_OVERFLOW; break; }
+        nt = nkeep + nnew;
         created += (uint32_t)nnew;
         wk.faces += (uint32_t)nnew;
         counter = counter + 1;
     }
     g.sync();
     r.depth = xmin_new;
-    // the contact point and everything after it (the force) are needed by one lane only: the others
-    // skip them, which keeps their FP64 operations (below and in contact_force) off the FP64 pipe
-    if (g.lane != 0) return;
-    const uint32_t t = indmin >= 0 ? m.ft[indmin] : indmin == -1 ? m.dt : m.ct;
-    const float4 fn = indmin >= 0 ? m.fn[indmin] : indmin == -1 ? m.dn : m.cn;
-    int a = ft_v(t, 0), b = ft_v(t, 1), c = ft_v(t, 2);
-    f3 n = xyz(fn);
-    f3 Pr = n * r.depth;
-    f3 Va = xyz(m.pv[a]), Vb = xyz(m.pv[b]), Vc = xyz(m.pv[c]);
-    f3 v0 = Vb - Va, v1 = Vc - Va, v2 = Pr - Va;
-    if (dot(cross(v0, v1), n) < 0.f) {
-        v0 = Vc - Va;
-        v1 = Vb - Va;
+    *wkp = wk;
+    if (g.lane == 0) epa_contact(m, hA, hB, xyz(fm), fc_v(tm, 0), fc_v(tm, 1), fc_v(tm, 2), r);
+    return r;
+}
+
+template <int LPP>
+__device__ __noinline__ EpaResult epa_compacting_call(const Group<LPP> g, EpaMem* mp, const float4* hA, int nA,
+                                                      const float4* hB, int nB, f3 S1, int a1, int b1, f3 S2, int a2,
+                                                      int b2, f3 S3, int a3, int b3, f3 S4, int a4, int b4, Work3* wkp)
+{
+    return epa_compacting<LPP>(g, mp, hA, nA, hB, nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, wkp);
+}
+
+// EPA of one pair in the single-pass kernel: the append-only list, and for the rare pair that outgrows
+// it, the compacting one (its work counted once: the first attempt's is dropped)
+template <int LPP>
+__device__ __forceinline__ void epa_run(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, const float4* hB,
+                                        int nB, f3 S1, int a1, int b1, f3 S2, int a2, int b2, f3 S3, int a3, int b3,
+                                        f3 S4, int a4, int b4, EpaResult& r, Work3& wk)
+{
+    const Work3 w0 = wk;
+    epa<LPP>(g, m, hA, nA, hB, nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, r, wk);
+    if (r.status & MWD_ST_EPA_OVERFLOW) {
+        wk = w0;
+        r = epa_compacting_call<LPP>(g, &m, hA, nA, hB, nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, &wk);
     }
-    float v00 = dot(v0, v0), v01 = dot(v0, v1), v11 = dot(v1, v1), v20 = dot(v2, v0), v21 = dot(v2, v1);
-    float den = v00 * v11 - v01 * v01;
-    float bv = (v11 * v20 - v01 * v21) / den;
-    float bw = (v00 * v21 - v01 * v20) / den;
-    float bu = (float)(1.0 - (double)bw - (double)bv);
-    int pa = m.pab[a], pb = m.pab[b], pc = m.pab[c];
-    r.fa[0] = pa & 0xff; r.fa[1] = pb & 0xff; r.fa[2] = pc & 0xff;
-    r.fb[0] = pa >> 8; r.fb[1] = pb >> 8; r.fb[2] = pc >> 8;
-    r.cpA = (xyz(hA[r.fa[0]]) * bu + xyz(hA[r.fa[1]]) * bv) + xyz(hA[r.fa[2]]) * bw;
-    r.cpB = (xyz(hB[r.fb[0]]) * bu + xyz(hB[r.fb[1]]) * bv) + xyz(hB[r.fb[2]]) * bw;
-    r.n = n;
 }
 
 struct ForceResult {
@@ -838,7 +980,7 @@ __device__ void process_pair(const NarrowArgs& a, int64_t P, const Group<LPP>& g
                     d4 = cross(S1, S2);
                     support<LPP>(g, hA, p.nA, hB, p.nB, d4, S4, a4, b4, wk);
                 }
-                epa<LPP>(g, em, hA, p.nA, hB, p.nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er, wk);
+                epa_run<LPP>(g, em, hA, p.nA, hB, p.nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er, wk);
                 if (leader) {
                     float imA, imB;
                     pair_inv_mass<MODE>(a, p, M, imA, imB);
@@ -1175,9 +1317,10 @@ __global__ void hist_flip_kernel(NarrowArgs a)
     if (threadIdx.x == 0 && blockIdx.x == 0) *a.hist_parity ^= 1;
 }
 
-// CorrectFlat, EPA, force and the outputs for EPA record i, by one group (em: its polytope; hull:
-// its staging area when the hulls are staged)
-template <int LPP>
+// CorrectFlat, EPA, force and the outputs for EPA record i, by one group (em: its polytope; hull: its
+// staging area when the hulls are staged).  RETRY: the record's face list overflowed in the EPA pass,
+// run it with the compacting EPA.
+template <int LPP, bool RETRY>
 __device__ __forceinline__ void epa_record(const NarrowArgs& a, const Group<LPP>& g, EpaMem* em, float4* hull,
                                            int64_t i)
 {
@@ -1185,58 +1328,82 @@ __device__ __forceinline__ void epa_record(const NarrowArgs& a, const Group<LPP>
     const SimplexRec* recs = reinterpret_cast<const SimplexRec*>(a.epa_rec);
     const SimplexRec rec = recs[i];
     const int64_t P = rec.P;
-    PairView p;
-    // the hulls staged in shared memory, or read in place from the (L1-cached) vertex table
+    // Only the hulls before the EPA: the pair's other inputs are loaded after it, by the lane that
+    // evaluates the force, so that the EPA loop holds fewer registers.  The hulls are staged in shared
+    // memory, or read in place from the (L1-cached) vertex table.  (GJK recorded the pair, so both
+    // hulls fit the staging area.)
+    const int2 pr = reinterpret_cast<const int2*>(a.pairs)[P];
+    const int oa = a.st.vert_off[pr.x], ob = a.st.vert_off[pr.y];
+    const int nA = a.st.vert_off[pr.x + 1] - oa, nB = a.st.vert_off[pr.y + 1] - ob;
     const float4* hA = hull;
     const float4* hB = hull + a.hull_cap;
-    load_pair<1>(a, P, p, hull, hull + a.hull_cap, g.lane, LPP, !a.epa_global);
     if (a.epa_global) {
-        hA = wv + a.st.vert_off[p.idA];
-        hB = wv + a.st.vert_off[p.idB];
-    }
-    if (a.hist_keys) {
-        p.dt = hist_get(a, p.idA, p.idB);
-        p.dtn = sqrtf(p.dt.x * p.dt.x + p.dt.y * p.dt.y + p.dt.z * p.dt.z);
+        hA = wv + oa;
+        hB = wv + ob;
+    } else {
+        for (int k = g.lane; k < nA; k += LPP) hull[k] = wv[oa + k];
+        for (int k = g.lane; k < nB; k += LPP) hull[a.hull_cap + k] = wv[ob + k];
     }
     g.sync();
-    const mwd_material& M = a.scenes[a.st.info[p.idA] >> 1].mat[p.wall];
     Work3 wk = {0u, 0u, 0u};
     f3 S1 = xyz(rec.S[0]), S2 = xyz(rec.S[1]), S3 = xyz(rec.S[2]), S4 = xyz(rec.S[3]);
     int a1 = rec.ia & 0xff, a2 = (rec.ia >> 8) & 0xff, a3 = (rec.ia >> 16) & 0xff, a4 = rec.ia >> 24;
     int b1 = rec.ib & 0xff, b2 = (rec.ib >> 8) & 0xff, b3 = (rec.ib >> 16) & 0xff, b4 = rec.ib >> 24;
     if (is_flat(S1, S2, S3, S4)) {
         f3 d4 = cross(S1, S2);
-        support<LPP>(g, hA, p.nA, hB, p.nB, d4, S4, a4, b4, wk);
+        support<LPP>(g, hA, nA, hB, nB, d4, S4, a4, b4, wk);
     }
     EpaResult er;
-    epa<LPP>(g, *em, hA, p.nA, hB, p.nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er, wk);
+    if (!RETRY)
+        epa<LPP>(g, *em, hA, nA, hB, nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, er, wk);
+    else
+        er = epa_compacting<LPP>(g, em, hA, nA, hB, nB, S1, a1, b1, S2, a2, b2, S3, a3, b3, S4, a4, b4, &wk);
     if (g.lane == 0) {
-        ForceResult fo;
-        float imA, imB;
-        pair_inv_mass<1>(a, p, M, imA, imB);
-        contact_force(p.cA, p.cB, er.depth, er.n, er.cpA, er.cpB, M, p.vA, p.vB, p.wA, p.wB, p.dt, p.qA, p.dtn,
-                      p.IsA, p.IsB, imA, imB, fo);
-        set_status(a.status, er.status);
-        if (a.hist_keys) hist_put(a, p.idA, p.idB, fo.dt);
-        if (a.det_out) {
-            float4* o = a.det_out + 3 * i;
-            o[0] = f4(fo.F, 0.f);
-            o[1] = f4(fo.TA, 0.f);
-            o[2] = f4(fo.TB, 0.f);
-        } else {
-            accumulate<1>(a, p, fo);
-        }
-        if (a.face_ids) {
-            int* fid = a.face_ids + 6 * P;
-            for (int k = 0; k < 3; ++k) {
-                fid[k] = er.fa[k];
-                fid[3 + k] = er.fb[k];
+        bool retry = false;
+        if (!RETRY && (er.status & MWD_ST_EPA_OVERFLOW)) {
+            // the face list outgrew FCAP: the record runs again with the compacting EPA after this
+            // pass (the list of such records permitting; otherwise the truncated result stands, flagged)
+            const int slot = atomicAdd(epa_retry_count(a), 1);
+            if (slot < EPA_RETRY_CAP) {
+                epa_retry_list(a)[slot] = (int32_t)i;
+                retry = true;
             }
         }
-        if (a.work_counters) {
-            atomicAdd(a.work_counters + 0, (unsigned long long)wk.dots);
-            atomicAdd(a.work_counters + 1, (unsigned long long)wk.faces);
-            atomicAdd(a.work_counters + 2, (unsigned long long)wk.queries);
+        if (!retry) {
+            PairView p;
+            load_pair<1>(a, P, p, nullptr, nullptr, 0, 1, false);
+            if (a.hist_keys) {
+                p.dt = hist_get(a, p.idA, p.idB);
+                p.dtn = sqrtf(p.dt.x * p.dt.x + p.dt.y * p.dt.y + p.dt.z * p.dt.z);
+            }
+            const mwd_material& M = a.scenes[a.st.info[p.idA] >> 1].mat[p.wall];
+            ForceResult fo;
+            float imA, imB;
+            pair_inv_mass<1>(a, p, M, imA, imB);
+            contact_force(p.cA, p.cB, er.depth, er.n, er.cpA, er.cpB, M, p.vA, p.vB, p.wA, p.wB, p.dt, p.qA, p.dtn,
+                          p.IsA, p.IsB, imA, imB, fo);
+            set_status(a.status, er.status);
+            if (a.hist_keys) hist_put(a, p.idA, p.idB, fo.dt);
+            if (a.det_out) {
+                float4* o = a.det_out + 3 * i;
+                o[0] = f4(fo.F, 0.f);
+                o[1] = f4(fo.TA, 0.f);
+                o[2] = f4(fo.TB, 0.f);
+            } else {
+                accumulate<1>(a, p, fo);
+            }
+            if (a.face_ids) {
+                int* fid = a.face_ids + 6 * P;
+                for (int k = 0; k < 3; ++k) {
+                    fid[k] = er.fa[k];
+                    fid[3 + k] = er.fb[k];
+                }
+            }
+            if (a.work_counters) {
+                atomicAdd(a.work_counters + 0, (unsigned long long)wk.dots);
+                atomicAdd(a.work_counters + 1, (unsigned long long)wk.faces);
+                atomicAdd(a.work_counters + 2, (unsigned long long)wk.queries);
+            }
         }
     }
     g.sync();
@@ -1287,9 +1454,31 @@ __global__ void __launch_bounds__(BT, 640 / BT) epa_pass_kernel(NarrowArgs a)
             e = b + size < m ? (int)b + size : m;
             seen = i - fixed + size;
         }
-        epa_record<LPP>(a, g, em, hull, i);
+        epa_record<LPP, false>(a, g, em, hull, i);
         i += step;
     }
+}
+
+// The records whose face list overflowed in the EPA pass, run again with the compacting EPA (a
+// separate kernel, so that the EPA pass itself carries none of that code; it finds an empty list almost
+// always and ends at once)
+template <int LPP, int BT>
+__global__ void __launch_bounds__(BT, 1) epa_retry_kernel(NarrowArgs a)
+{
+    pdl_wait();
+    pdl_launch_dependents();
+    extern __shared__ float4 smem[];
+    constexpr int GPB = BT / LPP;
+    const int grp = threadIdx.x / LPP;
+    Group<LPP> g;
+    g.lane = threadIdx.x % LPP;
+    g.mask = LPP == 32 ? 0xffffffffu : (((1u << LPP) - 1u) << ((threadIdx.x & 31) / LPP * LPP));
+    EpaMem* em = reinterpret_cast<EpaMem*>(smem) + grp;
+    float4* hull = reinterpret_cast<float4*>(reinterpret_cast<EpaMem*>(smem) + GPB) + (size_t)grp * 2 * a.hull_cap;
+    const int c = *epa_retry_count(a);
+    const int nr = c < EPA_RETRY_CAP ? c : EPA_RETRY_CAP;
+    for (int k = (int)blockIdx.x * GPB + grp; k < nr; k += (int)gridDim.x * GPB)
+        epa_record<LPP, true>(a, g, em, hull, epa_retry_list(a)[k]);
 }
 
 // threads per block of a block-size code of the lanes word (0: 128, 1: 64, 2: 256)
@@ -1324,6 +1513,11 @@ int launch_epa_bt(const NarrowArgs& a, cudaStream_t s)
     int rc = launch_setup(setup, epa_pass_kernel<LPP, BT>, BT, shm, 200 * 1024, &per_sm);
     if (rc) return rc;
     MWD_CUDA(launch_pdl(epa_pass_kernel<LPP, BT>, (unsigned)(num_sms() * per_sm), BT, shm, s, a));
+    static LaunchSetup retry_setup;
+    int retry_per_sm = 0;
+    rc = launch_setup(retry_setup, epa_retry_kernel<LPP, BT>, BT, shm, 200 * 1024, &retry_per_sm);
+    if (rc) return rc;
+    MWD_CUDA(launch_pdl(epa_retry_kernel<LPP, BT>, (unsigned)num_sms(), BT, shm, s, a));
     return MWD_OK;
 }
 
@@ -1416,7 +1610,7 @@ int launch_narrow_two_pass(const NarrowArgs& a, int lanes, cudaStream_t s)
         set_error("block-size code must be 0 (128 threads), 1 (64) or 2 (256) (got GJK %d, EPA %d)", gb, eb);
         return MWD_ERR_INVALID;
     }
-    if (!a.epa_zeroed) MWD_CUDA(cudaMemsetAsync(a.epa_count, 0, MWD_EPA_COUNT_INTS * sizeof(int32_t), s));
+    if (!a.epa_zeroed) MWD_CUDA(cudaMemsetAsync(a.epa_count, 0, 8 * sizeof(int32_t), s));
     if (a.hist_keys) MWD_CUDA(launch_pdl(hist_clear_kernel, (unsigned)(num_sms() * 4), 256, 0, s, a));
     int rc = MWD_OK;
     switch (gl) {

@@ -76,13 +76,68 @@ class PairScene:
 
         pos[:, 3] = rad_t[shape]  # bounding radius (rotation keeps the vertex norms)
         f32 = dict(dtype=torch.float32, device=dev)
+        vel = torch.cat([torch.randn((rows, 3), generator=g, **f32) * 0.5, torch.zeros((rows, 1), **f32)], 1)
+        w = torch.cat([torch.randn((rows, 3), generator=g, **f32) * 2.0, torch.zeros((rows, 1), **f32)], 1)
+        q = torch.cat([torch.ones((rows, 1), **f32), torch.zeros((rows, 3), **f32)], 1)
+        en = scene.restitution_from_damping(zeta)
+        self._assemble(pos, vel, w, q, torch.from_numpy(inert).to(dev)[shape].contiguous(),
+                       torch.from_numpy(inv).to(dev)[shape].contiguous(), off, body, world, int(V),
+                       dict(Kn=kn, en=en, et=en, mu=mu, Kn_wall=kn, en_wall=en, et_wall=en, mu_wall=mu,
+                            num_vertices_max=int(V), num_particles_wall=0, timestep=dt), two_pass)
+
+    @classmethod
+    def from_arrays(cls, inp, params, lanes=8, two_pass=True, device="cuda"):
+        """The pairs of per-pair arrays in the reference's layout (MWDiem.py:847-903; world-frame
+        vertices padded to V, as the oracle takes them), as the device step holds them: pair i is rows
+        (2i, 2i+1) with exactly those vertices, centres, velocities, spins and quaternions.  The narrow
+        phase then sees the oracle's inputs bit for bit.  `params`: the contact law (the reference's
+        constants; no walls)."""
+        self = cls.__new__(cls)
+        dev = torch.device(device)
+        P = int(np.asarray(inp["A_com"]).shape[0])
+        self.n_pairs = P
+        self.lanes = int(lanes)
+        rows = 2 * P
+
+        def inter(a, b, width):
+            out = np.zeros((rows, width), np.float64)
+            out[0::2, :np.asarray(a).shape[1]] = a
+            out[1::2, :np.asarray(b).shape[1]] = b
+            return out
+
+        com = inter(inp["A_com"], inp["B_com"], 4)
+        V = int(np.asarray(inp["A_verts"]).shape[1])
+        counts = np.empty(rows, np.int64)
+        counts[0::2], counts[1::2] = inp["A_nv"], inp["B_nv"]
+        verts = np.empty((rows, V, 3), np.float32)
+        verts[0::2], verts[1::2] = inp["A_verts"], inp["B_verts"]
+        mask = np.arange(V)[None, :] < counts[:, None]
+        world = np.zeros((int(counts.sum()), 4), np.float32)
+        world[:, :3] = verts[mask]
+        rel = verts.astype(np.float64) - com[:, None, :3]
+        com[:, 3] = np.sqrt((rel ** 2).sum(2) * mask).max(1)
+        off = np.zeros(rows + 1, np.int64)
+        off[1:] = np.cumsum(counts)
+        inert = np.zeros((rows, 4), np.float32)
+        inert[0::2, 3], inert[1::2, 3] = inp["IsA"], inp["IsB"]
+        f32 = dict(dtype=torch.float32, device=dev)
+        world_t = torch.from_numpy(world).to(dev)
+        self._assemble(torch.from_numpy(com).to(dev), torch.from_numpy(inter(inp["A_vel"], inp["B_vel"], 4)).to(**f32),
+                       torch.from_numpy(inter(inp["A_angvel"], inp["B_angvel"], 4)).to(**f32),
+                       torch.from_numpy(inter(inp["qA"], inp["qB"], 4)).to(**f32), torch.from_numpy(inert).to(dev),
+                       torch.ones((rows, 4), **f32), torch.from_numpy(off).to(dev), world_t.clone(), world_t, V,
+                       dict(params, num_particles_wall=0), two_pass)
+        return self
+
+    def _assemble(self, pos, vel, w, q, inertia, inv_inertia, off, body, world, V, params, two_pass):
+        """State, scene and work arrays of the rows (pair i = rows 2i, 2i+1) for mwd_narrow_force."""
+        dev = pos.device
+        rows = int(pos.shape[0])
+        total = int(world.shape[0])
+        f32 = dict(dtype=torch.float32, device=dev)
         t = {"pos": pos, "dx_all": torch.zeros((rows, 4), dtype=torch.float64, device=dev),
              "wall_normal": torch.zeros((rows, 4), dtype=torch.float64, device=dev),
-             "vel": torch.cat([torch.randn((rows, 3), generator=g, **f32) * 0.5, torch.zeros((rows, 1), **f32)], 1),
-             "w": torch.cat([torch.randn((rows, 3), generator=g, **f32) * 2.0, torch.zeros((rows, 1), **f32)], 1),
-             "q": torch.cat([torch.ones((rows, 1), **f32), torch.zeros((rows, 3), **f32)], 1),
-             "inertia": torch.from_numpy(inert).to(dev)[shape].contiguous(),
-             "inv_inertia": torch.from_numpy(inv).to(dev)[shape].contiguous(),
+             "vel": vel, "w": w, "q": q, "inertia": inertia, "inv_inertia": inv_inertia,
              "info": torch.zeros(rows, dtype=torch.int32, device=dev),
              "vert_off": off.to(torch.int32), "body_verts": body, "world_verts": world}
         for k in ("vel_half", "w_half_bf", "w_bf", "q_half", "q_all", "q_acc", "force", "torque", "ext_force",
@@ -96,13 +151,13 @@ class PairScene:
             setattr(st, k, t[k].data_ptr())
         st.n, st.n_verts, st.max_verts = rows, total, int(V)
         self.state = st
-        en = scene.restitution_from_damping(zeta)
+        p = params
         sc = (Scene * 1)()
-        sc[0].dt = dt
-        sc[0].law = ContactParams(kn, en, en, mu, kn, en, en, mu, dt, 0, 0, self.lanes, 0)
+        sc[0].dt = p["timestep"]
+        sc[0].law = ContactParams(p["Kn"], p["en"], p["et"], p["mu"], p["Kn_wall"], p["en_wall"], p["et_wall"],
+                                  p["mu_wall"], p["timestep"], 0, 0, self.lanes, 0)
         check(lib().mwd_derive_material(C.byref(sc[0].law), sc[0].mat))
-        self.params = dict(Kn=kn, en=en, et=en, mu=mu, Kn_wall=kn, en_wall=en, et_wall=en, mu_wall=mu,
-                           num_vertices_max=int(V), num_particles_wall=0, timestep=dt)
+        self.params = dict(p, num_vertices_max=int(V), num_particles_wall=0)
         self.scenes_host = sc
         raw = bytes(C.string_at(C.addressof(sc), C.sizeof(sc)))
         self.scenes_dev = torch.frombuffer(bytearray(raw), dtype=torch.uint8).to(dev)

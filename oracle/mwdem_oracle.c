@@ -24,7 +24,7 @@
 
 #define ORC_VCAP 64
 #define ORC_FCAP 4096      /* faces an EPA may create (storage; the reference's T[50] overflows at 50) */
-#define ORC_LIVE_CAP 128   /* faces alive at once: the CUDA kernel's compacted list (MWD_EPA_FACE_CAP) */
+#define ORC_LIVE_CAP 127   /* faces alive at once in the CUDA kernel's compacting EPA (MWD_EPA_FACE_CAP - 1) */
 #define ORC_DIAG 19
 #define ORC_NCOUNT 10
 #define ORC_ST_EPA_NOCONV 1

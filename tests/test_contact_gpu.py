@@ -211,3 +211,30 @@ def test_epa_beyond_128_faces_resolves_like_the_oracle(lanes):
     assert np.array_equal(g["collision"], o["collision"])
     assert bits_equal(g["diag"], o["diag"][:, :10])
     assert bits_equal(g["force"], o["force"]) and bits_equal(g["torque"], o["torque"])
+
+
+@pytest.mark.parametrize("lanes", [1 | (16 << 8) | (1 << 16), 8 | (32 << 8)])
+def test_epa_beyond_128_faces_in_the_two_pass_narrow_phase(lanes):
+    # the same pair in the device step's two-pass narrow phase: its EPA pass stops the pair when the
+    # append-only face list is full and a retry kernel runs it again with the compacting EPA; the
+    # result must be the oracle's, bit for bit, with the work counted once
+    from mwdiem_gb300.pairbench import PairScene
+    inp, N = make_pairs(2000, seed=242, V=64, n_min=32, n_max=64, dist=(0.3, 1.2))
+    p = dict(CONTACT_PARAMS, num_vertices_max=64)
+    sub = select(inp, np.arange(1040, 1070))
+    ps = PairScene.from_arrays(sub, p, lanes=lanes)
+    ps.narrow(count_work=True)
+    torch.cuda.synchronize()
+    P = 30
+    local = dict(sub, A_id=(2 * np.arange(P)).astype(np.int32), B_id=(2 * np.arange(P) + 1).astype(np.int32))
+    o = oracle.contact(local, p, 2 * P, "f32")
+    assert o["counters"][14, 9] == 129
+    assert not int(ps.w["status"].item()) & 2, "EPA_OVERFLOW"
+    assert np.array_equal(ps.w["collision"].cpu().numpy(), o["collision"])
+    assert bits_equal(ps.t["force"][:, :3].cpu().numpy(), o["force"])
+    assert bits_equal(ps.t["torque"][:, :3].cpu().numpy(), o["torque"])
+    got = tuple(int(x) for x in ps.w["counters"].cpu().numpy())
+    nsup = o["counters"][:, 0].astype(np.int64)
+    want = (int((nsup * (local["A_nv"].astype(np.int64) + local["B_nv"])).sum()),
+            int(o["counters"][:, 9][o["collision"] == 1].astype(np.int64).sum()), int(nsup.sum()))
+    assert got == want
