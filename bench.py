@@ -282,10 +282,11 @@ def main():
     V = sim.max_verts
     window = Window(sim, WINDOW_STEPS)
     from mwdiem_gb300 import autotune
-    tuning = {} if args.no_tune else autotune.tune_lanes(sim, steps=3)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    # tuned the way the step is timed: each step after an L2 flush
+    tuning = {} if args.no_tune else autotune.tune_lanes(sim, steps=6, flush=flush)
     sim.capture(steps_per_replay=1)
     window.restore()
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     # clocks are sampled every 20 ms from the start of the warm-up (kept under the same load for at
     # least 0.5 s, so the sampler is running) to the end of the timed region
     clocks = ClockSampler(local)

@@ -15,20 +15,34 @@ import copy
 import torch
 
 
-def time_steps(sim, steps=5, reps=3, per=1):
+def time_steps(sim, steps=5, reps=3, per=1, flush=None):
     """Median ms per graph-replayed step (after one captured warm-up step); `per` steps per graph
-    (rounded up to whole graphs)."""
+    (rounded up to whole graphs).  With `flush` (a tensor larger than L2), each graph replay is timed
+    on its own after the tensor is overwritten, outside the timed events: the regime of a step whose
+    state is not in L2."""
     sim.capture(per)
     n = max(1, -(-steps // per))
     stream = torch.cuda.current_stream()
     best = []
     for _ in range(reps):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        sim.replay(n)
-        e1.record(stream)
+        if flush is None:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sim.replay(n)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            best.append(e0.elapsed_time(e1) / (n * per))
+            continue
+        evs = []
+        for _ in range(n):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sim.replay(1)
+            e1.record(stream)
+            evs.append((e0, e1))
         torch.cuda.synchronize()
-        best.append(e0.elapsed_time(e1) / (n * per))
+        best.append(sum(a.elapsed_time(b) for a, b in evs) / (n * per))
     best.sort()
     return best[len(best) // 2]
 
@@ -65,17 +79,18 @@ def describe(lanes):
     return s
 
 
-def tune_lanes(sim, candidates=DEFAULT_CANDIDATES, steps=5, blocks=True):
+def tune_lanes(sim, candidates=DEFAULT_CANDIDATES, steps=5, blocks=True, flush=None):
     """Time the scene with each lanes-per-pair setting (GJK-pass lanes | EPA-pass lanes << 8) on a
     copy of its state, then the block sizes of the two passes at the fastest setting; set the fastest
-    on `sim`, and return {setting: ms per step}.  The state of `sim` is restored afterwards."""
+    on `sim`, and return {setting: ms per step}.  The state of `sim` is restored afterwards.  `flush`:
+    time every step with L2 overwritten first (time_steps)."""
     saved = {k: v.clone() for k, v in sim.t.items()}
     res = {}
 
     def run(lanes):
         sim.lanes = int(lanes)
         sim.graph = None
-        res[lanes] = time_steps(sim, steps)
+        res[lanes] = time_steps(sim, steps, flush=flush)
         for k, v in saved.items():
             sim.t[k].copy_(v)
 
