@@ -348,8 +348,12 @@ def main():
     sim.step_host(host, 1)
     torch.cuda.synchronize()
     e2e_value, _ = job_rate(host_steps(), N_PARTICLES * ne, world, "cuda")
-    e2e = {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-           "copies_around_step_graph": plain_value}
+    # bytes back to the host per step: the whole state by a copy, or the rows the integrator updates
+    # (the particles, 208 B each) when it writes them to the mapped host buffer itself
+    back = N_PARTICLES * (nbytes // sim.n) if sim.host_graph_mirrored else nbytes
+    e2e = {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": back,
+           "state_back": "written to the mapped host buffer by the integrator's row pass" if sim.host_graph_mirrored
+           else "copied after the integrator's row pass", "copies_around_step_graph": plain_value}
 
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,

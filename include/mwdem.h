@@ -354,6 +354,20 @@ int mwd_narrow_force(const mwd_state* st, const mwd_scene* scenes_dev, mwd_work*
  * rewrites world_verts, zeroes force/torque. */
 int mwd_integrate(mwd_state* st, const mwd_scene* scenes_dev, uint32_t* status, mwd_stream_t stream);
 
+/* The integrator's row pass (mwd_integrate_rows) that also writes every state array it updates --
+ * pos, dx_all, vel, vel_half, w_half_bf, w_bf, w, q, q_half, q_all, q_acc -- into `mirror`, a copy of
+ * the memory block `block` (block_bytes long, holding all of those arrays) in page-locked host memory
+ * the GPU can address (mwd_host_mapped), at the same offsets.  No reference counterpart: for a
+ * caller that keeps its state in host memory, as the reference's loop does (MWDiem.py:986-1001), the
+ * state returns to the host during the pass instead of by a copy after it.  Rows the pass leaves
+ * unchanged (walls, rows waiting at an inlet) are not written: the mirror must already hold them. */
+int mwd_integrate_rows_mirror(mwd_state* st, const mwd_scene* scenes_dev, uint32_t* status, void* mirror,
+                              const void* block, int64_t block_bytes, mwd_stream_t stream);
+
+/* Device address of page-locked host memory (cudaHostGetDevicePointer), for mwd_integrate_rows_mirror.
+ * Host utility; no reference counterpart. */
+int mwd_host_mapped(const void* host, void** device_address);
+
 /* mwd_integrate in two parts (a state with vert_owner and xform): the row pass (state, forces zeroed,
  * each row's transform into st->xform), then the vertex pass (world_verts from st->xform).  Between
  * the two the state is final, so a copy of it may run beside the vertex pass. */

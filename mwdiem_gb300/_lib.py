@@ -163,6 +163,8 @@ def lib():
             "mwd_refresh_vertices": (C.c_int, [C.POINTER(State), _P]),
             "mwd_integrate_rows": (C.c_int, [C.POINTER(State), _P, _P, _P]),
             "mwd_world_vertices": (C.c_int, [C.POINTER(State), _P]),
+            "mwd_integrate_rows_mirror": (C.c_int, [C.POINTER(State), _P, _P, _P, _P, i64, _P]),
+            "mwd_host_mapped": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
             "mwd_probe_fp32": (C.c_int, [i32, _P, C.POINTER(C.c_double), _P]),
             "mwd_contact_pairs_noalloc": (C.c_int, [i64, i32, i32] + [_P] * 20 +
                                           [C.POINTER(ContactParams), _P, _P, _P]),
@@ -185,7 +187,7 @@ def lib():
 EXPORTED = ("mwd_last_error", "mwd_version", "mwd_num_sms", "mwd_scan_tmp_ints", "mwd_derive_material",
             "mwd_contact_pairs", "mwd_verlet_ref", "mwd_cell_keys", "mwd_wall_pairs", "mwd_linked_cell_hash",
             "mwd_broadphase", "mwd_narrow_force", "mwd_integrate", "mwd_step", "mwd_refresh_vertices",
-            "mwd_integrate_rows", "mwd_world_vertices", "mwd_probe_fp32",
+            "mwd_integrate_rows", "mwd_world_vertices", "mwd_integrate_rows_mirror", "mwd_host_mapped", "mwd_probe_fp32",
             "mwd_contact_pairs_noalloc", "mwd_det_scratch_bytes", "mwd_inlet_step", "mwd_diff_collect", "mwd_diff_force", "mwd_diff_integrate",
             "mwd_diff_mirror", "mwd_diff_adjoint")
 

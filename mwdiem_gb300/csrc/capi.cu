@@ -601,6 +601,55 @@ int mwd_integrate_rows(mwd_state* st, const mwd_scene* scenes_dev, uint32_t* sta
     return launch_integrate(*st, scenes_dev, status, reinterpret_cast<cudaStream_t>(stream), false);
 }
 
+int mwd_integrate_rows_mirror(mwd_state* st, const mwd_scene* scenes_dev, uint32_t* status, void* mirror,
+                              const void* block, int64_t block_bytes, mwd_stream_t stream)
+{
+    if (!st || !scenes_dev || !st->vert_owner || !st->xform || !mirror || !block || block_bytes <= 0) {
+        set_error("mwd_integrate_rows_mirror: needs scenes, a state with vert_owner and xform, a mirror and its block");
+        return MWD_ERR_INVALID;
+    }
+    // every array the row pass writes (the force/torque accumulators aside) must lie in the block
+    const char* b0 = static_cast<const char*>(block);
+    const char* b1 = b0 + block_bytes;
+    const int64_t n = st->n;
+    const struct {
+        const void* p;
+        int64_t bytes;
+    } arrays[] = {{st->pos, 32 * n},      {st->dx_all, 32 * n}, {st->vel, 16 * n},    {st->vel_half, 16 * n},
+                  {st->w_half_bf, 16 * n}, {st->w_bf, 16 * n},   {st->w, 16 * n},      {st->q, 16 * n},
+                  {st->q_half, 16 * n},    {st->q_all, 16 * n},  {st->q_acc, 16 * n}};
+    for (const auto& a : arrays) {
+        const char* p = static_cast<const char*>(a.p);
+        if (!p || p < b0 || p + a.bytes > b1) {
+            set_error("mwd_integrate_rows_mirror: a state array lies outside the mirrored block");
+            return MWD_ERR_INVALID;
+        }
+    }
+    if ((reinterpret_cast<uintptr_t>(mirror) - reinterpret_cast<uintptr_t>(block)) & 31) {
+        set_error("mwd_integrate_rows_mirror: the mirror must have the block's alignment modulo 32 bytes");
+        return MWD_ERR_INVALID;
+    }
+    const int64_t delta = static_cast<const char*>(mirror) - b0;
+    return launch_integrate_rows_mirror(*st, scenes_dev, status, delta, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int mwd_host_mapped(const void* host, void** device_address)
+{
+    if (!host || !device_address) {
+        set_error("mwd_host_mapped: null argument");
+        return MWD_ERR_INVALID;
+    }
+    void* d = nullptr;
+    cudaError_t e = cudaHostGetDevicePointer(&d, const_cast<void*>(host), 0);
+    if (e != cudaSuccess || !d) {
+        cudaGetLastError();
+        set_error("mwd_host_mapped: not page-locked host memory mapped for the device (%s)", cudaGetErrorString(e));
+        return MWD_ERR_INVALID;
+    }
+    *device_address = d;
+    return MWD_OK;
+}
+
 int mwd_world_vertices(mwd_state* st, mwd_stream_t stream)
 {
     if (!st || !st->vert_owner || !st->xform) {

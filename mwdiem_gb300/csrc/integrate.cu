@@ -221,8 +221,11 @@ __device__ __forceinline__ float4 rot_increment(f3 w, float s)
 }
 
 // one row's update (walls: unchanged); returns the centre and q_acc the vertex pass uses
+// MIRROR: every state array written here is also written `mirror` bytes further on, into a copy of the
+// state block that lives in host memory the GPU can reach (the force/torque accumulators excepted)
+template <bool MIRROR = false>
 __device__ __forceinline__ void row_update(const mwd_state& st, const mwd_scene* __restrict__ scenes, int P,
-                                           dpos& pos_out, float4& qacc_out)
+                                           dpos& pos_out, float4& qacc_out, int64_t mirror = 0)
 {
     const int info = st.info[P];
     dpos pos = reinterpret_cast<const dpos*>(st.pos)[P];
@@ -282,17 +285,25 @@ __device__ __forceinline__ void row_update(const mwd_state& st, const mwd_scene*
             np = pos;
         }
         pos = np;
-        reinterpret_cast<dpos*>(st.pos)[P] = pos;
-        reinterpret_cast<dpos*>(st.dx_all)[P] = dxall;
-        st4(st.vel, P, f4(v, 0.f));
-        st4(st.vel_half, P, f4(vh, 0.f));
-        st4(st.w_half_bf, P, f4(whbf, 0.f));
-        st4(st.w_bf, P, f4(wbf, 0.f));
-        st4(st.w, P, f4(w, 0.f));
-        st4(st.q, P, q);
-        st4(st.q_half, P, qh);
-        st4(st.q_all, P, qall);
-        st4(st.q_acc, P, qacc);
+        auto putd = [&](double* a, const dpos& x) {
+            reinterpret_cast<dpos*>(a)[P] = x;
+            if (MIRROR) reinterpret_cast<dpos*>(reinterpret_cast<char*>(a) + mirror)[P] = x;
+        };
+        auto put4 = [&](float* a, float4 x) {
+            st4(a, P, x);
+            if (MIRROR) st4(reinterpret_cast<float*>(reinterpret_cast<char*>(a) + mirror), P, x);
+        };
+        putd(st.pos, pos);
+        putd(st.dx_all, dxall);
+        put4(st.vel, f4(v, 0.f));
+        put4(st.vel_half, f4(vh, 0.f));
+        put4(st.w_half_bf, f4(whbf, 0.f));
+        put4(st.w_bf, f4(wbf, 0.f));
+        put4(st.w, f4(w, 0.f));
+        put4(st.q, q);
+        put4(st.q_half, qh);
+        put4(st.q_all, qall);
+        put4(st.q_acc, qacc);
         st4(st.force, P, make_float4(0.f, 0.f, 0.f, 0.f));
         st4(st.torque, P, make_float4(0.f, 0.f, 0.f, 0.f));
     }
@@ -367,9 +378,11 @@ __global__ void __launch_bounds__(RB) integrate_kernel(mwd_state st, const mwd_s
     }
 }
 
-// the row pass of the split integrator: one thread per row, the transform to st.xform
+// the row pass of the split integrator: one thread per row, the transform to st.xform (MIRROR: the
+// state also written into its copy in GPU-reachable host memory, `mirror` bytes further on)
+template <bool MIRROR>
 __global__ void __launch_bounds__(RB) integrate_rows_kernel(mwd_state st, const mwd_scene* __restrict__ scenes,
-                                                            uint32_t* status)
+                                                            uint32_t* status, int64_t mirror)
 {
     pdl_wait();
     pdl_launch_dependents();
@@ -377,7 +390,7 @@ __global__ void __launch_bounds__(RB) integrate_rows_kernel(mwd_state st, const 
     if (P >= st.n) return;
     dpos pos;
     float4 qacc;
-    row_update(st, scenes, P, pos, qacc);
+    row_update<MIRROR>(st, scenes, P, pos, qacc, mirror);
     float x[16];
     row_xform(qacc, pos, x, x + 9);
     x[15] = 0.f;
@@ -445,12 +458,22 @@ int launch_refresh_vertices(const mwd_state& st, cudaStream_t s)
     return launch_world_verts(st, s);
 }
 
+int launch_integrate_rows_mirror(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, int64_t mirror,
+                                 cudaStream_t s)
+{
+    if (st.n <= 0) return MWD_OK;
+    MWD_CUDA(launch_pdl(integrate_rows_kernel<true>, (st.n + RB - 1) / RB, RB, 0, s, st, scenes, status, mirror));
+    MWD_CUDA(cudaGetLastError());
+    return MWD_OK;
+}
+
 int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, cudaStream_t s,
                      bool with_verts)
 {
     if (st.n <= 0) return MWD_OK;
     if (st.vert_owner && st.xform) {
-        MWD_CUDA(launch_pdl(integrate_rows_kernel, (st.n + RB - 1) / RB, RB, 0, s, st, scenes, status));
+        MWD_CUDA(launch_pdl(integrate_rows_kernel<false>, (st.n + RB - 1) / RB, RB, 0, s, st, scenes, status,
+                            (int64_t)0));
         if (with_verts && st.n_verts > 0)
             MWD_CUDA(launch_pdl(world_verts_kernel, (st.n_verts + 255) / 256, 256, 0, s, st));
     } else {

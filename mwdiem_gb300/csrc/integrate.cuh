@@ -23,6 +23,9 @@ int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* sta
                      bool with_verts = true);
 // world vertices from st.xform (row transforms) through st.vert_owner, one thread per vertex
 int launch_world_verts(const mwd_state& st, cudaStream_t s);
+// the row pass, every state array it writes also written `mirror` bytes further on
+int launch_integrate_rows_mirror(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, int64_t mirror,
+                                 cudaStream_t s);
 // row transforms + world vertices from the current state (no integration)
 int launch_refresh_vertices(const mwd_state& st, cudaStream_t s);
 

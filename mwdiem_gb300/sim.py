@@ -473,19 +473,29 @@ class Simulator:
         host["_buffer"].copy_(self.mutable, non_blocking=True)
         return host
 
-    def capture_host(self, host):
+    def host_mapped(self, host):
+        """Device address of the pinned buffer of `host` (from host_state), or None when the GPU cannot
+        address it directly."""
+        dp = C.c_void_p()
+        rc = lib().mwd_host_mapped(C.c_void_p(host["_buffer"].data_ptr()), C.byref(dp))
+        return dp.value if rc == 0 else None
+
+    def capture_host(self, host, mirror=True):
         """Capture one step between the pinned buffers of `host` (from host_state) in one CUDA graph,
         replayed by step_host(host, 1).  The centres, the first array of the state, are copied in
         first and the broad phase (which reads no other array of the state) starts on them while the
         rest of the state is copied in on a second stream; the narrow phase waits for that copy.  The
-        state goes back to `host` after the integrator's row pass, beside its vertex pass.  The same
-        kernels as step(): the same results.  Not with an inlet (its rows enter inside mwd_step)."""
+        state returns to `host` during the integrator's row pass, which writes each updated row both to
+        the device and to the host buffer (mwd_integrate_rows_mirror; `mirror`, and the buffer mapped
+        for the device), or else by a copy after that pass, beside its vertex pass.  The same kernels as
+        step(): the same results.  Not with an inlet (its rows enter inside mwd_step)."""
         if self.inlet is not None:
             raise ValueError("capture_host: the inlet runs inside mwd_step; use step_host without capture")
         hb = host["_buffer"]
         if hb.device.type != "cpu" or not hb.is_pinned() or hb.dtype != self.mutable.dtype or \
                 hb.numel() != self.mutable.numel():
             raise ValueError("capture_host: `host` must come from this simulator's host_state()")
+        mapped = self.host_mapped(host) if mirror else None
         self.step_host(host, 1)  # warm-up outside capture
         torch.cuda.synchronize()
         npos = self.t["pos"].numel() * self.t["pos"].element_size()
@@ -500,14 +510,22 @@ class Simulator:
             self.broadphase()
             main.wait_stream(side)
             self.narrow_force()
-            self.integrate_rows()
-            side.wait_stream(main)
-            with torch.cuda.stream(side):
-                hb.copy_(self.mutable, non_blocking=True)
-            self.world_vertices()
-            main.wait_stream(side)
+            if mapped is not None:
+                check(lib().mwd_integrate_rows_mirror(C.byref(self.state), self.scenes_dev.data_ptr(),
+                                                      self.w["status"].data_ptr(), C.c_void_p(mapped),
+                                                      self.mutable.data_ptr(), self.mutable.numel(),
+                                                      _dev.stream_handle()))
+                self.world_vertices()
+            else:
+                self.integrate_rows()
+                side.wait_stream(main)
+                with torch.cuda.stream(side):
+                    hb.copy_(self.mutable, non_blocking=True)
+                self.world_vertices()
+                main.wait_stream(side)
         self.host_graph = g
         self.host_graph_buffer = hb
+        self.host_graph_mirrored = mapped is not None
         return g
 
     # ------------------------------------------------------------------ inspection

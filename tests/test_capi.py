@@ -43,3 +43,31 @@ def test_errors_are_codes_not_aborts():
     rc = _lib.lib().mwd_contact_pairs(-1, 8, 1, *([None] * 20), None, None, None, None)
     assert rc == _lib.MWD_ERR_INVALID
     assert b"bad arguments" in _lib.lib().mwd_last_error()
+
+
+def test_mirrored_row_pass_checks_its_block():
+    # mwd_integrate_rows_mirror rejects, before any device call, a state array outside the mirrored
+    # block and a mirror whose offset from the block is not a multiple of 32 bytes
+    import ctypes
+    import numpy as np
+    from mwdiem_gb300 import _lib
+    n = 4
+    block = np.zeros(208 * n + 64, np.uint8)
+    base = (block.ctypes.data + 31) // 32 * 32
+    st = _lib.State()
+    st.n = n
+    off = 0
+    for name, width in (("pos", 32), ("dx_all", 32), ("vel", 16), ("vel_half", 16), ("w_half_bf", 16),
+                        ("w_bf", 16), ("w", 16), ("q", 16), ("q_half", 16), ("q_all", 16), ("q_acc", 16)):
+        setattr(st, name, base + off)
+        off += width * n
+    st.vert_owner = st.xform = base      # only checked for presence before the launch
+    scenes = mirror = base               # never dereferenced on these paths
+    h = _lib.lib()
+    rc = h.mwd_integrate_rows_mirror(ctypes.byref(st), scenes, None, mirror + 4096, base, off - 16, None)
+    assert rc == _lib.MWD_ERR_INVALID and b"outside" in h.mwd_last_error()
+    rc = h.mwd_integrate_rows_mirror(ctypes.byref(st), scenes, None, mirror + 4096 + 16, base, off, None)
+    assert rc == _lib.MWD_ERR_INVALID and b"alignment" in h.mwd_last_error()
+    st.xform = None
+    rc = h.mwd_integrate_rows_mirror(ctypes.byref(st), scenes, None, mirror, base, off, None)
+    assert rc == _lib.MWD_ERR_INVALID

@@ -104,15 +104,18 @@ def test_host_round_trip_matches_device_stepping():
         assert torch.equal(host[k], b.t[k].cpu()), k
 
 
-def test_host_graph_matches_device_stepping():
+@pytest.mark.parametrize("mirror", [True, False])
+def test_host_graph_matches_device_stepping(mirror):
     # the captured host step (centres copied in first, the broad phase overlapping the copy of the
-    # rest of the state) gives the state of plain device steps, bit for bit (deterministic sums)
+    # rest of the state; the state back through the integrator's mirrored writes or by a copy) gives
+    # the state of plain device steps, bit for bit (deterministic sums)
     from mwdiem_gb300.sim import Simulator
     sp = dense_scene(n=300, seed=8, spacing=2.3, vel=0.2)
     a = Simulator(sp, deterministic=True)
     b = Simulator(sp, deterministic=True)
     host = a.host_state()
-    a.capture_host(host)         # one warm-up step through the plain host path
+    a.capture_host(host, mirror=mirror)         # one warm-up step through the plain host path
+    assert a.host_graph_mirrored == mirror
     for _ in range(6):
         a.step_host(host, 1)     # graph replays
     b.step(7)
