@@ -8,8 +8,8 @@
 //
 //   assign   key -> dense cell index (per scene key range), atomic count per cell
 //   scan     exclusive scan of the counts = cell-start table (a one-digit radix/counting sort)
-//   scatter  rows into their cell's slot range (atomicSub brings the counts back to zero)
-//   order    each cell's members sorted by id, then put in CPython 3.12 set iteration order
+//   place    rows into their cell's slot range, each shared cell's members sorted by id and then
+//            put in CPython 3.12 set iteration order by its last-arriving member (counts back to zero)
 //   count    per row: wall candidates + later members of its cell + members of the 7 neighbours
 //   scan     exclusive scan of the counts = output offsets
 //   emit     the same walk, writing [A, B] pairs
@@ -372,23 +372,6 @@ __global__ void assign_kernel(BroadArgs a)
     }
 }
 
-__global__ void scatter_kernel(BroadArgs a)
-{
-    pdl_wait();
-    pdl_launch_dependents();
-    if (a.tile_sums) {  // read by the cell scan, which has finished: zero for the next broad phase
-        const int64_t nb = (a.total_cells + SCAN_TILE - 1) / SCAN_TILE;
-        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nb; i += (int64_t)gridDim.x * blockDim.x)
-            a.tile_sums[i] = 0;
-    }
-    const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= a.row_hi) return;
-    const int g = a.cell_of[r];
-    if (g < 0) return;
-    const int slot = atomicSub(a.cell_count + g, 1) - 1;
-    a.scatter_out[a.cell_start[g] + slot] = r;
-}
-
 // write row v at sorted position i of cell g, with its centre/radius and cell alongside
 __device__ __forceinline__ void place(const BroadArgs& a, int i, int v, int g)
 {
@@ -400,32 +383,13 @@ __device__ __forceinline__ void place(const BroadArgs& a, int i, int v, int g)
     }
 }
 
-// one row of the order pass: singletons placed, small cells ordered by their smallest member's thread;
-// returns the cell to the caller when it is crowded (its smallest member's thread), else -1
-__device__ __forceinline__ int order_row(const BroadArgs& a, int r)
+// members of cell g (k of them, from scatter_out[s..s+k), written by other threads of this grid and
+// read past L1) ranked by id, then written in set order
+__device__ __forceinline__ void order_small_cell(const BroadArgs& a, int g, int s, int k)
 {
-    if (r >= a.row_hi) return -1;
-    // the row's own centre, loaded beside its cell lookups (most rows are alone in their cell)
-    double4 pr = make_double4(0.0, 0.0, 0.0, 0.0);
-    if (a.sorted_pos) pr = reinterpret_cast<const double4*>(a.pos)[r];
-    const int g = a.cell_of[r];
-    if (g < 0) return -1;
-    const int s = a.cell_start[g], e = a.cell_start[g + 1];
-    const int k = e - s;
-    if (k == 1) {
-        a.sorted[s] = r;
-        if (a.sorted_pos) {
-            a.sorted_pos[s] = make_float4((float)pr.x, (float)pr.y, (float)pr.z, (float)pr.w);
-            a.sorted_cell[s] = g;
-        }
-        return -1;
-    }
-    for (int j = s; j < e; ++j)
-        if (a.scatter_out[j] < r) return -1;  // the smallest id of the cell orders it
-    if (k > SMALL_CELL) return g;
     int m[SMALL_CELL];
     for (int j = 0; j < k; ++j) {
-        int v = a.scatter_out[s + j];
+        int v = __ldcg(a.scatter_out + s + j);
         int i = j;
         while (i > 0 && m[i - 1] > v) {
             m[i] = m[i - 1];
@@ -436,29 +400,75 @@ __device__ __forceinline__ int order_row(const BroadArgs& a, int r)
     int o[SMALL_CELL];
     int tab[SMALL_TAB], tmp[SMALL_TAB];
     unsigned char used[SMALL_TAB], used2[SMALL_TAB];
-    const int base = a.info ? a.scenes[scene_of(a, r)].row_begin : 0;
+    const int base = a.info ? a.scenes[scene_of(a, m[0])].row_begin : 0;
     pyset_order<SMALL_TAB>(m, k, o, tab, used, tmp, used2, base);
     for (int j = 0; j < k; ++j) place(a, s + j, o[j], g);
-    return -1;
 }
 
-// the order pass: every row of the block, then the block's crowded cells (more than SMALL_CELL
-// members, usually none) by its first warp -- members ranked by id in parallel, lane 0 replaying the
-// set inserts with the table in shared memory
-constexpr int ORDER_THREADS = 128;
-__global__ void __launch_bounds__(ORDER_THREADS) order_kernel(BroadArgs a)
+// The place pass: every row into its cell's range of the sorted list (the counting sort's scatter)
+// and each cell's members into CPython set order, in one kernel.  A row alone in its cell (most rows)
+// is written at its cell's start and the cell's count set back to zero.  The members of a shared
+// cell claim slots with atomicSub on the cell's count (low 16 bits, counting down to zero), write
+// themselves into scatter_out, and then add 1 << 16 to the same word: the member whose add finds
+// k - 1 earlier ones (every member's write made visible by the fence before its add) orders the
+// cell, in its own thread up to SMALL_CELL members, else by the first warp of its block with the
+// tables in shared memory; it sets the count back to zero.  A cell of more than 65,535 members
+// (beyond the packed count) is written in claim order and flagged, as are cells beyond BIG_CELL,
+// which are written in ascending ids.
+constexpr int PLACE_THREADS = 128;
+constexpr int PACKED_MAX = 0xffff;
+__global__ void __launch_bounds__(PLACE_THREADS) place_kernel(BroadArgs a)
 {
     pdl_wait();
     pdl_launch_dependents();
-    __shared__ int s_crowd[ORDER_THREADS];
+    __shared__ int s_crowd[PLACE_THREADS];
     __shared__ int s_nc;
     if (threadIdx.x == 0) s_nc = 0;
+    if (a.tile_sums) {  // read by the cell scan, which has finished: zero for the next broad phase
+        const int64_t nb = (a.total_cells + SCAN_TILE - 1) / SCAN_TILE;
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nb; i += (int64_t)gridDim.x * blockDim.x)
+            a.tile_sums[i] = 0;
+    }
     __syncthreads();
-    const int g0 = order_row(a, a.row_lo + blockIdx.x * blockDim.x + threadIdx.x);
-    if (g0 >= 0) s_crowd[atomicAdd(&s_nc, 1)] = g0;
+    const int r = a.row_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < a.row_hi) {
+        // the row's own centre, loaded beside its cell lookups (most rows are alone in their cell)
+        double4 pr = make_double4(0.0, 0.0, 0.0, 0.0);
+        if (a.sorted_pos) pr = reinterpret_cast<const double4*>(a.pos)[r];
+        const int g = a.cell_of[r];
+        if (g >= 0) {
+            const int s = a.cell_start[g], k = a.cell_start[g + 1] - s;
+            if (k == 1) {
+                a.cell_count[g] = 0;
+                a.sorted[s] = r;
+                if (a.sorted_pos) {
+                    a.sorted_pos[s] = make_float4((float)pr.x, (float)pr.y, (float)pr.z, (float)pr.w);
+                    a.sorted_cell[s] = g;
+                }
+            } else if (k > PACKED_MAX) {
+                const int slot = atomicSub(a.cell_count + g, 1) - 1;
+                place(a, s + slot, r, g);
+                if (slot == 0) set_status(a.status, MWD_ST_CELL_CROWDED);
+            } else {
+                unsigned* w = reinterpret_cast<unsigned*>(a.cell_count + g);
+                const int slot = (int)(atomicSub(w, 1u) & 0xffffu) - 1;
+                a.scatter_out[s + slot] = r;
+                __threadfence();
+                const unsigned before = atomicAdd(w, 0x10000u) >> 16;
+                if ((int)before == k - 1) {
+                    __threadfence();
+                    *w = 0u;
+                    if (k <= SMALL_CELL) order_small_cell(a, g, s, k);
+                    else s_crowd[atomicAdd(&s_nc, 1)] = g;
+                }
+            }
+        }
+    }
     __syncthreads();
     const int nc = s_nc;
     if (nc == 0 || threadIdx.x >= 32) return;
+    // the block's crowded cells, one at a time by its first warp: members ranked by id in parallel,
+    // lane 0 replaying the set inserts with the table in shared memory
     __shared__ int m[BIG_CELL];
     __shared__ int o[BIG_CELL];
     __shared__ int tab[BIG_TAB], tmp[BIG_TAB];
@@ -470,8 +480,8 @@ __global__ void __launch_bounds__(ORDER_THREADS) order_kernel(BroadArgs a)
         if (k > BIG_CELL) {
             // beyond the emulated table size: ascending ids, flagged
             for (int j = threadIdx.x; j < k; j += 32) {
-                int v = a.scatter_out[s + j], rank = 0;
-                for (int i = 0; i < k; ++i) rank += a.scatter_out[s + i] < v;
+                int v = __ldcg(a.scatter_out + s + j), rank = 0;
+                for (int i = 0; i < k; ++i) rank += __ldcg(a.scatter_out + s + i) < v;
                 place(a, s + rank, v, g);
             }
             if (threadIdx.x == 0) set_status(a.status, MWD_ST_CELL_CROWDED);
@@ -479,8 +489,8 @@ __global__ void __launch_bounds__(ORDER_THREADS) order_kernel(BroadArgs a)
             continue;
         }
         for (int j = threadIdx.x; j < k; j += 32) {
-            int v = a.scatter_out[s + j], rank = 0;
-            for (int i = 0; i < k; ++i) rank += a.scatter_out[s + i] < v;
+            int v = __ldcg(a.scatter_out + s + j), rank = 0;
+            for (int i = 0; i < k; ++i) rank += __ldcg(a.scatter_out + s + i) < v;
             m[rank] = v;
         }
         __syncwarp();
@@ -500,6 +510,13 @@ struct WallStage {
     int scene;        // the scene they belong to (-1: nothing staged)
     int nw;
 };
+
+// the reference's forward stencil in linear keys, o = 0..6: +1, +nx, +nx*ny, +nx*ny+1, +nx*ny+1+nx,
+// +nx*ny+nx, +nx+1 (LIBRARY_Coarse_contact_detection.py:96-129), from bit masks (no local array)
+__device__ __forceinline__ int64_t forward_offset(int o, int64_t nx, int64_t nxy)
+{
+    return (((0x3c >> o) & 1) ? nxy : 0) + (((0x72 >> o) & 1) ? nx : 0) + ((0x59 >> o) & 1);
+}
 
 // every candidate of the row at sorted position t (row r, cell g), passed to sink(A, B).
 // ws: optional float copies of the row's scene walls for the wall-distance test.
@@ -566,9 +583,8 @@ __device__ __forceinline__ void walk_pairs(const BroadArgs& a, int t, int r, int
     // forward neighbours
     const int64_t local = (int64_t)g - sc.cell_base;
     const int64_t nx = sc.nx, nxy = sc.nx * sc.ny;
-    const int64_t offs[7] = {1, nx, nxy, nxy + 1, nxy + 1 + nx, nxy + nx, nx + 1};
     if (part > 0) {
-        const int64_t l2 = local + offs[part - 1];
+        const int64_t l2 = local + forward_offset(part - 1, nx, nxy);
         if (l2 < 0 || l2 >= sc.n_keys) return;
         const int g2 = (int)(sc.cell_base + l2);
         const int e2 = a.cell_start[g2 + 1];
@@ -579,7 +595,7 @@ __device__ __forceinline__ void walk_pairs(const BroadArgs& a, int t, int r, int
     int rs[7], re[7];
 #pragma unroll
     for (int o = 0; o < 7; ++o) {
-        const int64_t l2 = local + offs[o];
+        const int64_t l2 = local + forward_offset(o, nx, nxy);
         rs[o] = re[o] = 0;
         if (l2 < 0 || l2 >= sc.n_keys) continue;
         const int g2 = (int)(sc.cell_base + l2);
@@ -816,8 +832,7 @@ int launch_broad(const BroadArgs& a, cudaStream_t s)
         rc = launch_scan(a.cell_count, a.total_cells, a.cell_start, a.scan_tmp, nullptr, INT64_MAX, nullptr, 0, s);
         if (rc) return rc;
     }
-    MWD_CUDA(launch_pdl(scatter_kernel, blocks(rows, T), T, 0, s, a));
-    MWD_CUDA(launch_pdl(order_kernel, blocks(rows, ORDER_THREADS), ORDER_THREADS, 0, s, a));
+    MWD_CUDA(launch_pdl(place_kernel, blocks(rows, PLACE_THREADS), PLACE_THREADS, 0, s, a));
     // rows that have a cell are at most `rows`; threads past cell_start[total] exit
     if (a.append) {
         // split each row's walk over APPEND_PARTS threads while the rows alone leave the GPU short of

@@ -33,7 +33,7 @@ struct BroadArgs {
     int64_t total_cells;
     int64_t pair_cap;
     int32_t* tile_sums;          // optional: per-scan-tile cell counts, added to by assign_kernel, read by
-                                 // the cell scan (no reduce pass) and zeroed by scatter_kernel
+                                 // the cell scan (no reduce pass) and zeroed by place_kernel
     int32_t walk_parts;          // append mode: threads per row (1, or 8: walls + own cell, 7 neighbours)
     int32_t pad2_;
 };
