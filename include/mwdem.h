@@ -302,7 +302,10 @@ typedef struct {
     int32_t cull_pairs;    /* 1: the broad phase lists only pairs whose bounding spheres (pos.w) overlap
                               within a rounding margin -- the others are exactly the candidates the
                               reference's first GJK test rejects; 0: the reference's full candidate list */
-    int32_t pad;
+    int32_t cell_table;    /* layout of cell_count / cell_start: 0 automatic (dense), 1 dense (a count
+                              and a start per cell), 2 occupancy-compressed where it fits (a bit per
+                              cell, counts and starts per occupied cell, carved out of the same two
+                              arrays; needs total_cells >= 4 n + 4096).  The same pairs either way. */
     int64_t total_cells;
     int64_t pair_cap;
     int32_t* face_ids;     /* optional (pair_cap, 6): support-vertex indices (into each row's vertex table)
@@ -333,6 +336,10 @@ int64_t mwd_det_scratch_bytes(int32_t n, int64_t epa_cap);
  * as many again for the per-tile cell counts the device-resident broad phase keeps between its
  * assign pass and its cell scan (zero on entry and on exit; allocate zeroed). */
 int64_t mwd_scan_tmp_ints(int64_t n);
+
+/* The cell table mwd_broadphase uses for n rows, total_cells cells and mwd_work.cell_table = mode:
+ * 1 dense, 2 occupancy-compressed.  Host utility; no reference counterpart. */
+int32_t mwd_cell_table(int64_t n, int64_t total_cells, int32_t mode);
 
 /* One broad phase over all scenes (rows of every scene; walls excluded from the cell hash). */
 int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes_host,

@@ -56,6 +56,10 @@ class ContactParams(C.Structure):
                 ("law", C.c_int32), ("pad", C.c_int32)]
 
 
+CELL_TABLE_AUTO = 0
+CELL_TABLE_DENSE = 1
+CELL_TABLE_COMPRESSED = 2
+
 LAW_REFERENCE = 0
 LAW_PHYSICAL = 1
 
@@ -96,7 +100,7 @@ class Work(C.Structure):
                                   "scan_tmp", "n_pairs", "status", "collision")] + \
                [("work_counters", _P), ("epa_count", _P), ("epa_rec", _P),
                 ("epa_cap", C.c_int64), ("sorted_pos", _P), ("sorted_cell", _P), ("cull_pairs", C.c_int32),
-                ("pad", C.c_int32), ("total_cells", C.c_int64),
+                ("cell_table", C.c_int32), ("total_cells", C.c_int64),
                 ("pair_cap", C.c_int64), ("face_ids", _P), ("deterministic", C.c_int32),
                 ("pad2", C.c_int32), ("det_scratch", _P), ("hist_cap", C.c_int64), ("hist_keys", _P),
                 ("hist_vals", _P), ("hist_parity", _P), ("inlet", _P)]
@@ -150,6 +154,7 @@ def lib():
             "mwd_version": (C.c_int, []),
             "mwd_num_sms": (i32, []),
             "mwd_scan_tmp_ints": (i64, [i64]),
+            "mwd_cell_table": (i32, [i64, i64, i32]),
             "mwd_derive_material": (C.c_int, [C.POINTER(ContactParams), C.POINTER(Material)]),
             "mwd_contact_pairs": (C.c_int, [i64, i32, i32] + [_P] * 20 + [C.POINTER(ContactParams), _P, _P, _P]),
             "mwd_verlet_ref": (C.c_int, [i32] + [_P] * 16 + [C.POINTER(VerletParams), _P, _P]),
@@ -184,7 +189,7 @@ def lib():
         return h
 
 
-EXPORTED = ("mwd_last_error", "mwd_version", "mwd_num_sms", "mwd_scan_tmp_ints", "mwd_derive_material",
+EXPORTED = ("mwd_last_error", "mwd_version", "mwd_num_sms", "mwd_scan_tmp_ints", "mwd_cell_table", "mwd_derive_material",
             "mwd_contact_pairs", "mwd_verlet_ref", "mwd_cell_keys", "mwd_wall_pairs", "mwd_linked_cell_hash",
             "mwd_broadphase", "mwd_narrow_force", "mwd_integrate", "mwd_step", "mwd_refresh_vertices",
             "mwd_integrate_rows", "mwd_world_vertices", "mwd_integrate_rows_mirror", "mwd_host_mapped", "mwd_probe_fp32",

@@ -35,7 +35,13 @@ struct BroadArgs {
     int32_t* tile_sums;          // optional: per-scan-tile cell counts, added to by assign_kernel, read by
                                  // the cell scan (no reduce pass) and zeroed by place_kernel
     int32_t walk_parts;          // append mode: threads per row (1, or 8: walls + own cell, 7 neighbours)
-    int32_t pad2_;
+    // occupancy-compressed cell table (sparse = 1; needs tile_sums): a bit per cell of the dense
+    // table, the cells' ranks among the occupied ones, and counts and starts per occupied cell, all
+    // carved out of cell_count and cell_start (launch_broad sets these)
+    int32_t sparse;
+    int32_t n_words;             // bitmap words, ceil(total_cells / 32)
+    int32_t words_pad;           // n_words + 1 rounded up to a multiple of 4: start of the next array
+    int32_t compact_len;         // entries of the per-occupied-cell counts (rows + 1, rounded up to 4)
 };
 
 int64_t scan_tmp_ints(int64_t n);
@@ -43,6 +49,9 @@ int64_t scan_tile_sums_offset(int64_t n);  // where the persistent cell-tile cou
 int launch_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* tmp, int64_t* total_out, int64_t cap,
                 uint32_t* status, uint32_t overflow_bit, cudaStream_t s);
 int launch_broad(const BroadArgs& a, cudaStream_t s);
+// 1 when launch_broad would use the occupancy-compressed table for these sizes (mode: 0 automatic,
+// 1 dense, 2 compressed where it fits)
+int broad_sparse(int64_t rows, int64_t total_cells, int64_t tile_sum_ints, int mode);
 int launch_keys(int N, const double* com, double csx, double csy, double csz, int64_t nx, int64_t ny, int64_t* keys,
                 cudaStream_t s);
 int launch_minmax(const int64_t* keys, int lo, int hi, unsigned long long* mm, cudaStream_t s);

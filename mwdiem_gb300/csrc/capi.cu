@@ -233,6 +233,12 @@ const char* mwd_last_error(void) { return g_err; }
 int mwd_version(void) { return 1; }
 int32_t mwd_num_sms(void) { return num_sms(); }
 int64_t mwd_scan_tmp_ints(int64_t n) { return scan_tmp_ints(n); }
+
+int32_t mwd_cell_table(int64_t n, int64_t total_cells, int32_t mode)
+{
+    const int64_t m = (total_cells > n ? total_cells : n) + 1;
+    return broad_sparse(n, total_cells, scan_tmp_ints(m) - scan_tile_sums_offset(m), mode) ? 2 : 1;
+}
 int64_t mwd_det_scratch_bytes(int32_t n, int64_t epa_cap)
 {
     return n < 0 || epa_cap < 0 ? -1 : (int64_t)det_scratch_bytes(n, epa_cap);
@@ -497,6 +503,8 @@ int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_s
         const int64_t rows = (int64_t)st->n;
         const int64_t m = (work->total_cells > rows ? work->total_cells : rows) + 1;
         a.tile_sums = work->scan_tmp + scan_tile_sums_offset(m);
+        a.sparse = broad_sparse(rows, work->total_cells, scan_tmp_ints(m) - scan_tile_sums_offset(m),
+                                work->cell_table);
     }
     return launch_broad(a, reinterpret_cast<cudaStream_t>(stream));
 }

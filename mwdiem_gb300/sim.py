@@ -15,8 +15,9 @@ import numpy as np
 import torch
 
 from . import _dev
-from ._lib import (EPA_COUNT_INTS, HULL_CAP, INFO_INACTIVE, LAW_PHYSICAL, LAW_REFERENCE, ST_PAIR_OVERFLOW, ContactParams, Inlet,
-                   Material, MwdError, Scene, State, Work, check, lib, status_names)
+from ._lib import (CELL_TABLE_AUTO, CELL_TABLE_COMPRESSED, CELL_TABLE_DENSE, EPA_COUNT_INTS, HULL_CAP, INFO_INACTIVE,
+                   LAW_PHYSICAL, LAW_REFERENCE, ST_PAIR_OVERFLOW, ContactParams, Inlet, Material, MwdError, Scene,
+                   State, Work, check, lib, status_names)
 from .scene import CompactBodies, SceneSpec
 
 CONTACT_LAWS = {"reference": LAW_REFERENCE, "physical": LAW_PHYSICAL}
@@ -52,7 +53,7 @@ class Layout:
 
 class Simulator:
     def __init__(self, scenes, lanes=8, pair_cap=None, device="cuda", collect_collisions=False, two_pass=True,
-                 cull_pairs=True, deterministic=False, persistent_history=False, inlet=None):
+                 cull_pairs=True, deterministic=False, persistent_history=False, inlet=None, cell_table="auto"):
         _dev.require_cuda()
         if isinstance(scenes, SceneSpec):
             scenes = [scenes]
@@ -65,6 +66,15 @@ class Simulator:
         self.cull_pairs = bool(cull_pairs)
         self.deterministic = bool(deterministic)
         self.persistent_history = bool(persistent_history)
+        # the broad phase's cell table: "dense" (a count and a start per cell), "compressed" (a bit per
+        # cell, counts and starts per occupied cell; where it fits), or "auto" (dense, the faster of
+        # the two on every workload measured): the same pairs either way
+        tables = {"auto": CELL_TABLE_AUTO, "dense": CELL_TABLE_DENSE, "compressed": CELL_TABLE_COMPRESSED}
+        if cell_table not in tables:
+            raise ValueError(f"cell_table must be one of {sorted(tables)}")
+        self.cell_table = tables[cell_table]
+        compressed = lib().mwd_cell_table(self.n, self.total_cells, self.cell_table) == 2
+        self.cell_table_in_use = "compressed" if compressed else "dense"
         if (self.deterministic or self.persistent_history) and not self.two_pass:
             raise ValueError("deterministic accumulation and persistent history need the two-pass narrow phase")
         self._build_work(pair_cap, collect_collisions)
@@ -325,6 +335,7 @@ class Simulator:
             wk.epa_rec = w["epa_rec"].data_ptr()
             wk.epa_cap = cap
         wk.cull_pairs = 1 if self.cull_pairs else 0
+        wk.cell_table = self.cell_table
         w["sorted_pos"] = torch.zeros((n, 4), dtype=torch.float32, device=self.device)
         w["sorted_cell"] = torch.zeros(n, **i32)
         wk.sorted_pos = w["sorted_pos"].data_ptr()

@@ -2,7 +2,8 @@
 
   * pour20k: bench.py's own scene (20,000 hulls, its 140,005-cell table scanned tile by tile), at
     step 0 and after 25 graph-replayed steps, with both lane settings the autotuner picks for it;
-  * a batch of 16 scenes (one of 50,000 particles; cubes, tetrahedra and hulls) in one state;
+  * a batch of 16 scenes (one of 50,000 particles; cubes, tetrahedra and hulls) in one state, with
+    the dense and with the occupancy-compressed cell table;
   * the narrow-phase workload of 4M independent random pairs: a sample of 131,072 pairs;
   * the kernel's own work counters (the roofline's numerator) against the oracle's per-pair counts.
 
@@ -143,13 +144,15 @@ def test_pour20k_bench_scene_matches_oracle(lanes):
     print(f"pour20k lanes {lanes:#x}: contacts {contacts0} at step 0, {contacts25} at step 26")
 
 
-def test_batched_subset_matches_oracle():
+@pytest.mark.parametrize("table", ["dense", "compressed"])
+def test_batched_subset_matches_oracle(table):
+    # the broad phase with either cell table (automatic: dense)
     from mwdiem_gb300.sim import Simulator
     specs = scene.batched_scenes(n_scenes=1, total=50_000, n_lo=50_000, n_hi=50_000, seed=11) + \
         scene.batched_scenes(n_scenes=15, total=60_000, seed=12)
     assert max(sp.n_particles for sp in specs) == 50_000
-    sim = Simulator(specs, collect_collisions=True, cull_pairs=True)
-    assert sim.total_cells > 65536
+    sim = Simulator(specs, collect_collisions=True, cull_pairs=True, cell_table=table)
+    assert sim.total_cells > 65536 and sim.cell_table_in_use == table
     for step in range(2):
         full = device_pairs(sim, cull=False)
         cut = device_pairs(sim, cull=True)
@@ -174,6 +177,29 @@ def test_batched_subset_matches_oracle():
         sim.step(3)
         torch.cuda.synchronize()
     sim.check_status()
+
+
+def test_compressed_cell_table_lists_the_dense_tables_pairs():
+    # pour20k with both cell tables in deterministic mode (the list in cell order): the same sorted
+    # rows, the same pair lists entry for entry, and the same states step after step
+    from mwdiem_gb300.sim import Simulator
+    spec = bench.build_scene(bench.SCENE["seed"])
+    a = Simulator(spec, cull_pairs=True, deterministic=True, cell_table="dense")
+    b = Simulator(spec, cull_pairs=True, deterministic=True, cell_table="compressed")
+    assert a.cell_table_in_use == "dense" and b.cell_table_in_use == "compressed"
+    assert Simulator(spec).cell_table_in_use == "dense"   # automatic: the dense table
+    for _ in range(3):
+        for cull in (False, True):
+            pa, pb = device_pairs(a, cull), device_pairs(b, cull)
+            assert len(pa) > 1000 and np.array_equal(pa, pb)
+            assert torch.equal(a.w["sorted"], b.w["sorted"])
+        assert int(b.w["cell_count"].abs().sum()) == 0   # left zero, as the dense table's counts
+        a.step(10)
+        b.step(10)
+        for k in a.MUTABLE:
+            assert torch.equal(a.t[k], b.t[k]), k
+    a.check_status()
+    b.check_status()
 
 
 def test_narrow_4m_pairs_sample_matches_oracle():
