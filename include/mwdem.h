@@ -101,6 +101,8 @@ typedef struct {
     double inv_mu;
     double KtA;
     int32_t physical; /* MWD_LAW_PHYSICAL: tc, Gn, Kt, Gt per pair from the masses (see above) */
+    float inv_mu_hi, inv_mu_lo; /* inv_mu as a float pair: hi = (float)inv_mu, lo = (float)(inv_mu - hi) */
+    float KtA_hi, KtA_lo;       /* KtA likewise (the kernel's float-float evaluation of Kt and Gt) */
     int32_t pad;
 } mwd_material;
 

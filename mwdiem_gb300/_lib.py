@@ -68,6 +68,7 @@ class Material(C.Structure):
     _fields_ = [("Kn_f", C.c_float), ("mu_f", C.c_float), ("Gn", C.c_float), ("ln_et", C.c_float),
                 ("dt_f", C.c_float), ("ln_en", C.c_float), ("Xn", C.c_float), ("Xt", C.c_float),
                 ("mu", C.c_double), ("inv_mu", C.c_double), ("KtA", C.c_double), ("physical", C.c_int32),
+                ("inv_mu_hi", C.c_float), ("inv_mu_lo", C.c_float), ("KtA_hi", C.c_float), ("KtA_lo", C.c_float),
                 ("pad", C.c_int32)]
 
 

@@ -129,6 +129,10 @@ static void derive_one(double Kn, double en, double et, double mu, double dt, in
     m->inv_mu = 1 / mu;
     m->KtA = Kn * (double)Xet / (double)Xen;
     m->physical = law == MWD_LAW_PHYSICAL ? 1 : 0;
+    m->inv_mu_hi = (float)m->inv_mu;
+    m->inv_mu_lo = (float)(m->inv_mu - (double)m->inv_mu_hi);
+    m->KtA_hi = (float)m->KtA;
+    m->KtA_lo = (float)(m->KtA - (double)m->KtA_hi);
     m->pad = 0;
 }
 

@@ -277,6 +277,130 @@ __device__ __forceinline__ bool epa_converged(float x, float p)
     return (double)x * 1.00001 > (double)p && (double)x * 0.99999 < (double)p;
 }
 
+// ---------------------------------------------------------------- the reference's double results in FP32
+// A few per-contact quantities the reference computes in double and rounds to float (the barycentric
+// weight of the contact point, .cu:583; the tangential stiffness and damping, .cu:746-749; the Coulomb
+// test, .cu:774).  FP64 runs at a small fraction of the FP32 rate on this GPU and its long latency sat
+// on every contact's path, so they are evaluated in float-float arithmetic (error-free sums, fused
+// multiply-add remainders) and the float is taken when it is provably the double computation's result
+// rounded to float: when the value lies farther from a float rounding boundary than the error bound of
+// both computations.  Otherwise (a value within ~2^-18 of a boundary, or non-finite or extreme
+// operands) the double computation runs.
+
+// s + e = a + b exactly (Knuth)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// s + e = a + b exactly, for |a| >= |b| (or a = 0) (Dekker)
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    e = b - (s - a);
+}
+
+// true when every real within `err` of a + b rounds to the float a (round to nearest): |b| plus the
+// error stays below half the spacing of the floats next to a on b's side (the spacing below a power
+// of two, toward zero, is half the one above).  False for |a| outside [2^-102, 2^127) and non-finite a.
+__device__ __forceinline__ bool rounds_to(float a, float b, float err)
+{
+    const uint32_t ua = __float_as_uint(a) & 0x7fffffffu;
+    if (ua < 0x0c800000u || ua >= 0x7f000000u) return false;
+    const float ulp = __uint_as_float(ua & 0x7f800000u) * 1.1920928955078125e-7f;  // 2^(exponent - 23)
+    const bool toward_zero = (b < 0.f) != (a < 0.f);
+    const float half = ((ua & 0x007fffffu) == 0u && toward_zero) ? 0.25f * ulp : 0.5f * ulp;
+    return fabsf(b) + err < half * 0.99999f;
+}
+
+// spacing of the floats at x (2^-149 for subnormal x, +inf for 0 and non-finite x)
+__device__ __forceinline__ float ulp_of(float x)
+{
+    const uint32_t ux = __float_as_uint(x) & 0x7fffffffu;
+    if (ux == 0u || ux >= 0x7f800000u) return __int_as_float(0x7f800000);
+    if (ux < 0x00800000u) return 1.401298464324817e-45f;
+    return __uint_as_float(ux & 0x7f800000u) * 1.1920928955078125e-7f;
+}
+
+// (float)(1.0 - (double)bw - (double)bv).  The exact value is s2 + t + r (error-free sums) and a is the
+// float nearest to s2 + t.  1, bw and bv are multiples of q = the smallest of their spacings, and so
+// are 1 - bw and the result: below 2^53 q the double computation holds both exactly, and with r = 0 a is
+// then its result rounded to float, ties included.  Otherwise a is certified against the double
+// computation's error, at most 2^-53 (|1 - bw| + |result|).
+__device__ __forceinline__ float one_minus_two(float bw, float bv)
+{
+    float s1, e1, s2, e2, t, r, a, b0;
+    two_sum(1.f, -bw, s1, e1);
+    two_sum(s1, -bv, s2, e2);
+    two_sum(e2, e1, t, r);
+    two_sum(s2, t, a, b0);
+    if (fabsf(bw) < 1e30f && fabsf(bv) < 1e30f) {
+        const float q = fminf(fminf(ulp_of(bw), ulp_of(bv)), 1.1920928955078125e-7f);
+        const bool exact = fmaxf(fabsf(s1), fabsf(a)) < q * 2251799813685248.f;  // 2^51 q
+        if (exact && r == 0.f) return a;
+        const float b = b0 + r;
+        const float err = (exact ? 0.f : (fabsf(s1) + fabsf(a)) * 2.220446049250313e-16f) +
+                          fabsf(b) * 1.1920928955078125e-7f;
+        if (rounds_to(a, b, err)) return a;
+    }
+    return (float)(1.0 - (double)bw - (double)bv);
+}
+
+// Kt = (float)(KtA * 1 / C) and Gt = (float)((-1) * 2 / C * (double)ln_et) with
+// C = inv_mu + (double)x + (double)y (.cu:746-749; x, y the float quotients dA^2/IsA, dB^2/IsB).  C is
+// formed as a float pair from non-negative terms; each quotient is a rounded float quotient (KtA_hi / ch,
+// and -2 / ch as -2 RN(1 / ch), exact scaling), whose remainder a fused multiply-add gives exactly,
+// corrected by that remainder times RN(1 / ch).  The pair values are within 2^-43 of the exact ones
+// and the double results within 5 * 2^-53 of them: a margin of 2^-41 certifies the float.
+__device__ __forceinline__ void tangential_coeffs(const mwd_material& M, float x, float y, float& Kt, float& Gt)
+{
+    bool okK = false, okG = false;
+    if (x >= 0.f && x < 1e30f && y >= 0.f && y < 1e30f && M.inv_mu_hi > 0.f && M.inv_mu_hi < 1e30f) {
+        float c1, e1, c2, e2, ch, cl;
+        two_sum(M.inv_mu_hi, x, c1, e1);
+        two_sum(c1, y, c2, e2);
+        fast_two_sum(c2, (M.inv_mu_lo + e1) + e2, ch, cl);
+        const float rc = 1.f / ch;
+        // (KtA_hi + KtA_lo) / (ch + cl)
+        const float q1 = M.KtA_hi / ch;
+        const float rq = ((fmaf(-q1, ch, M.KtA_hi) + M.KtA_lo) - q1 * cl) * rc;
+        float kh, kl;
+        fast_two_sum(q1, rq, kh, kl);
+        // -2 / (ch + cl), then times ln_et
+        const float g1 = -2.f * rc;
+        const float rg = (fmaf(-g1, ch, -2.f) - g1 * cl) * rc;
+        float gh, gl;
+        fast_two_sum(g1, rg, gh, gl);
+        const float p = gh * M.ln_et;
+        float Gh, Gl;
+        fast_two_sum(p, fmaf(gh, M.ln_et, -p) + gl * M.ln_et, Gh, Gl);
+        okK = rounds_to(kh, kl, fabsf(kh) * 4.547473508864641e-13f);  // 2^-41
+        okG = rounds_to(Gh, Gl, fabsf(Gh) * 4.547473508864641e-13f);
+        Kt = kh;
+        Gt = Gh;
+    }
+    if (okK && okG) return;
+    const double C = M.inv_mu + (double)x + (double)y;
+    if (!okK) Kt = (float)(M.KtA * 1 / C);
+    if (!okG) Gt = (float)((-1) * 2 / C * (double)M.ln_et);
+}
+
+// (double)Ftn > mu * (double)Fnn (.cu:774): 1 when greater, 0 when not greater, -1 when unordered (NaN).
+// mu_f * Fnn is within 2.1 u of the double product (u = 2^-24): a margin of 4e-7 (~6.7 u) decides.
+__device__ __forceinline__ int coulomb_compare(float Ftn, float Fnn, const mwd_material& M)
+{
+    const float t = M.mu_f * Fnn;
+    if (t >= 1e-30f && t <= 1e30f) {
+        const float e = t * 4e-7f;
+        if (Ftn > t + e) return 1;
+        if (Ftn < t - e) return 0;
+    }
+    const double X = (double)Ftn, P = M.mu * (double)Fnn;
+    return X > P ? 1 : (X <= P ? 0 : -1);
+}
+
 // AddTriangle (.cu:270-325): normal and distance of the face (e0, e1, e2), its winding (t1, t2) and
 // validity (1, or -2 with distance 1e30 when the origin's projection falls outside it)
 __device__ __forceinline__ float4 face_geom(const EpaMem& m, int e0, int e1, int e2, int& t1, int& t2, int& valid)
@@ -471,7 +595,7 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
     float den = v00 * v11 - v01 * v01;
     float bv = (v11 * v20 - v01 * v21) / den;
     float bw = (v00 * v21 - v01 * v20) / den;
-    float bu = (float)(1.0 - (double)bw - (double)bv);
+    float bu = one_minus_two(bw, bv);
     int pa = m.pab[a], pb = m.pab[b], pc = m.pab[c];
     r.fa[0] = pa & 0xff; r.fa[1] = pb & 0xff; r.fa[2] = pc & 0xff;
     r.fb[0] = pa >> 8; r.fb[1] = pb >> 8; r.fb[2] = pc >> 8;
@@ -512,7 +636,7 @@ __device__ __forceinline__ void epa_contact(const EpaMem& m, const float4* hA, c
     float den = v00 * v11 - v01 * v01;
     float bv = (v11 * v20 - v01 * v21) / den;
     float bw = (v00 * v21 - v01 * v20) / den;
-    float bu = (float)(1.0 - (double)bw - (double)bv);
+    float bu = one_minus_two(bw, bv);
     int pa = m.pab[a], pb = m.pab[b], pc = m.pab[c];
     r.fa[0] = pa & 0xff; r.fa[1] = pb & 0xff; r.fa[2] = pc & 0xff;
     r.fb[0] = pa >> 8; r.fb[1] = pb >> 8; r.fb[2] = pc >> 8;
@@ -730,9 +854,7 @@ __device__ __forceinline__ void contact_force(f3 cA, f3 cB, float depth, f3 n, f
         f3 dA = cp - cA, dB = cp - cB;
         float dA2 = dA.x * dA.x + dA.y * dA.y + dA.z * dA.z;
         float dB2 = dB.x * dB.x + dB.y * dB.y + dB.z * dB.z;
-        double C = M.inv_mu + (double)(dA2 / IsA) + (double)(dB2 / IsB);
-        Kt = (float)(M.KtA * 1 / C);
-        Gt = (float)((-1) * 2 / C * (double)M.ln_et);
+        tangential_coeffs(M, dA2 / IsA, dB2 / IsB, Kt, Gt);
         Gn = M.Gn;
     } else {
         // effective masses from the pair; tc and the dampings follow from them (MWD_LAW_PHYSICAL)
@@ -768,8 +890,9 @@ __device__ __forceinline__ void contact_force(f3 cA, f3 cB, float depth, f3 n, f
     f3 Ft = dt * (-1.f) * Kt - ut * Gt;
     float Ftn = sqrtf(Ft.x * Ft.x + Ft.y * Ft.y + Ft.z * Ft.z);
     // two separate tests as in the reference, so a NaN norm takes the second (slip) branch
-    if ((double)Ftn > M.mu * (double)Fnn) Ft = ((tij * Fnn) * (-1.f)) * M.mu_f;
-    if ((double)Ftn <= M.mu * (double)Fnn) {
+    const int coulomb = coulomb_compare(Ftn, Fnn, M);
+    if (coulomb == 1) Ft = ((tij * Fnn) * (-1.f)) * M.mu_f;
+    if (coulomb == 0) {
         float4 qi = qconj(qA);
         o.dt = qtrip(qA, dt, qi) + ut * M.dt_f;
     } else {
