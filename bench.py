@@ -56,11 +56,11 @@ class host_prints_to_stderr:
 METRIC = "particle-steps/s"
 WINDOW_STEPS = 500  # the pour configuration runs 500 steps
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one GJK-pass and one EPA-pass
-# launch of this step, from one capture of the eager first step: 5.180 MB + 0.163 MB (the writes stay
+# launch of this step, from one capture of the eager first step: 5.185 MB + 0.169 MB (the writes stay
 # in L2).  ncu cannot run inside this timing, so the figure is carried here.
-NARROW_DRAM_BYTES_PER_LAUNCH = 5.179648e6 + 0.163328e6
-# broad phase 5 (assign, cell scan, scatter, order, append) + GJK pass + EPA pass + integrator rows
-# + vertices
+NARROW_DRAM_BYTES_PER_LAUNCH = 5.184512e6 + 0.169472e6
+# broad phase 4 (assign, cell scan, place, append) + GJK pass + EPA pass + EPA overflow reruns +
+# integrator rows + vertices
 KERNELS_PER_STEP = 9
 
 
@@ -213,6 +213,11 @@ def narrow_flops(sim):
     the dot product) plus ~60 per EPA face built (cross product, normalisation, inside test)."""
     dots, faces, queries = sim.count_narrow_work()
     return 5.0 * dots + 60.0 * faces, dict(vertex_dots=dots, epa_faces=faces, support_queries=queries)
+
+
+def lib_integrate_kernels(n):
+    from mwdiem_gb300._lib import lib
+    return int(lib().mwd_integrate_kernels(int(n)))
 
 
 def integrate_bytes(sim):
@@ -491,7 +496,7 @@ def breakdown(sim, V, flush, reps=10):
         n, P = sim.n, sim.n_pairs()
         bbytes = n * (32 + 4 + 4 + 4 + 4 + 4 + 8) + sim.total_cells * 12 + P * (8 + 8 + 8)
         a = bbytes / (ms["broad"] * 1e-3) / 1e9
-        roof = {"kernel": "broad phase (5 kernels)", "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s",
+        roof = {"kernel": "broad phase (4 kernels)", "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s",
                 "frac": a / hbm, "traffic": None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in pk else "fallback 6800"}
     return out, roof
@@ -765,7 +770,8 @@ def batch_stages(sim, reps=5):
     hbm = peaks().get("hbm_gbs", 6800.0)
     ib = integrate_bytes(sim)
     a = ib / (ms["integrate"] * 1e-3) / 1e9
-    return {"ms": ms, "integrate_roofline": {"kernel": "integrate_rows_kernel + world_verts_kernel", "bound": "hbm",
+    one = lib_integrate_kernels(sim.n) == 1
+    return {"ms": ms, "integrate_roofline": {"kernel": "integrate_kernel" if one else "integrate_rows_kernel + world_verts_kernel", "bound": "hbm",
                                             "bytes_per_step": ib, "achieved": a, "peak": hbm, "unit": "GB/s",
                                             "frac": a / hbm}}
 

@@ -238,7 +238,9 @@ typedef struct {
     int32_t max_verts;       /* largest vertex count of any row (<= MWD_HULL_CAP) */
     int32_t pad;
     const int32_t* vert_owner; /* optional (nv,) row of each vertex; with xform the integrator rewrites
-                                  the world vertices one thread per vertex (NULL: one block per 128 rows) */
+                                  the world vertices one thread per vertex up to the row count
+                                  mwd_integrate_kernels gives 1 for (NULL, or above it: one block per
+                                  128 rows and their vertices) */
     float* xform;            /* optional (n,16) scratch: R(q_acc) row-major, then the centre as float
                                 hi + lo per axis */
 } mwd_state;
@@ -339,6 +341,13 @@ int64_t mwd_det_scratch_bytes(int32_t n, int64_t epa_cap);
  * assign pass and its cell scan (zero on entry and on exit; allocate zeroed). */
 int64_t mwd_scan_tmp_ints(int64_t n);
 
+/* Kernels mwd_integrate launches for n rows of a state with vert_owner and xform: 2 (the row pass,
+ * then one thread per vertex) or 1 (each block's rows, then their vertices: from two full waves of
+ * blocks up, where the transforms' and vertex owners' trips through memory cost more than the
+ * vertex pass's spread).  In the one-kernel case st->xform is not written and mwd_step runs its steps
+ * without the vertex pass overlap.  Host utility; no reference counterpart. */
+int32_t mwd_integrate_kernels(int64_t n);
+
 /* The cell table mwd_broadphase uses for n rows, total_cells cells and mwd_work.cell_table = mode:
  * 1 dense, 2 occupancy-compressed.  Host utility; no reference counterpart. */
 int32_t mwd_cell_table(int64_t n, int64_t total_cells, int32_t mode);
@@ -388,7 +397,8 @@ int mwd_world_vertices(mwd_state* st, mwd_stream_t stream);
 int mwd_refresh_vertices(mwd_state* st, mwd_stream_t stream);
 
 /* broad phase + narrow phase + integrator, n_steps times.  With n_steps > 1 (and a state with
- * vert_owner and xform, no inlet) the world-vertex pass of each step but the last runs during the
+ * vert_owner and xform, no inlet, and a row count for which mwd_integrate_kernels gives 2) the
+ * world-vertex pass of each step but the last runs during the
  * next step's broad phase, on a second stream of the library's (one per device and calling thread)
  * that is joined before the narrow phase: the same results, and the state is complete when the
  * call's work on `stream` ends.

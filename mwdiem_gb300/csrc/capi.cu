@@ -238,6 +238,8 @@ int mwd_version(void) { return 1; }
 int32_t mwd_num_sms(void) { return num_sms(); }
 int64_t mwd_scan_tmp_ints(int64_t n) { return scan_tmp_ints(n); }
 
+int32_t mwd_integrate_kernels(int64_t n) { return integrate_in_one_kernel(n) ? 1 : 2; }
+
 int32_t mwd_cell_table(int64_t n, int64_t total_cells, int32_t mode)
 {
     const int64_t m = (total_cells > n ? total_cells : n) + 1;
@@ -692,7 +694,9 @@ int mwd_step(mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes
     const SideStream* side = nullptr;
     if (!work->inlet && st->vert_owner && st->xform && st->n > 0 && st->n_verts > 0 && overlap_enabled())
         side = side_stream(s);
-    const bool ovl = side && n_steps > 1;
+    // (the vertex pass overlaps the next broad phase only where the integrator runs it as a pass of its
+    // own; for row counts that take the one-kernel integrator the plain loop is faster)
+    const bool ovl = side && n_steps > 1 && !integrate_in_one_kernel(st->n);
     for (int i = 0; i < n_steps; ++i) {
         if (work->inlet) {
             int rc0 = mwd_inlet_step(st, work->inlet, stream);

@@ -21,6 +21,8 @@ int launch_verlet_ref(const VerletRefArgs& a, cudaStream_t s);
 // then rewritten from st.xform by a later launch_world_verts
 int launch_integrate(const mwd_state& st, const mwd_scene* scenes, uint32_t* status, cudaStream_t s,
                      bool with_verts = true);
+// true when launch_integrate with vertices runs one kernel for n rows (rows, then their vertices)
+bool integrate_in_one_kernel(int64_t n);
 // world vertices from st.xform (row transforms) through st.vert_owner, one thread per vertex
 int launch_world_verts(const mwd_state& st, cudaStream_t s);
 // the row pass, every state array it writes also written `mirror` bytes further on

@@ -188,6 +188,38 @@ def test_multi_step_overlap_is_exact():
             assert np.array_equal(ta, o.t[k].cpu().numpy(), equal_nan=True), k
 
 
+def test_one_kernel_integrator_matches_two_passes():
+    # from two full waves of blocks the integrator updates each block's rows and then their vertices in
+    # one kernel; it must give the bits of the row pass + vertex pass, and a ten-step call (which then
+    # runs without the vertex-pass overlap) those of ten one-step calls
+    from mwdiem_gb300 import _lib
+    from mwdiem_gb300.sim import Simulator
+    specs = scene.batched_scenes(n_scenes=10, total=340_000, n_lo=34_000, n_hi=34_000, seed=5)
+    a = Simulator(specs, deterministic=True)
+    b = Simulator(specs, deterministic=True)
+    assert _lib.lib().mwd_integrate_kernels(a.n) == 1 and _lib.lib().mwd_integrate_kernels(20_000) == 2
+    for _ in range(3):
+        for s in (a, b):
+            s.broadphase()
+            s.narrow_force()
+        a.integrate()
+        b.integrate_rows()
+        b.world_vertices()
+        torch.cuda.synchronize()
+        for k in a.MUTABLE + ("force", "torque", "world_verts"):
+            assert torch.equal(a.t[k], b.t[k]), k
+    assert a.n_pairs() > 1000
+    c = Simulator(specs, deterministic=True)
+    d = Simulator(specs, deterministic=True)
+    c.step(10)
+    for _ in range(10):
+        d.step(1)
+    torch.cuda.synchronize()
+    for k in ("pos", "q", "vel", "w", "world_verts"):
+        assert torch.equal(c.t[k], d.t[k]), k
+    a.check_status()
+
+
 def test_multi_step_calls_from_two_threads():
     # two host threads, each stepping its own simulator ten steps per call on its own stream (each
     # thread has its own overlap stream and events): the bits of the same calls made one after another
