@@ -310,6 +310,23 @@ __device__ bool pyset_order(const int* m, int k, int* out, int* tab, unsigned ch
     return true;
 }
 
+// list({lo, hi}) in CPython 3.12 (lo < hi inserted in that order, ids hashed as id - base): true when lo
+// comes first.  Two entries leave the 8-slot table unresized, and no slot index i has i + 9 <= 7, so a
+// collision goes straight to perturbation (pyset_order with k = 2); once the perturbation has shifted
+// out, i -> 5 i + 1 (mod 8) visits every slot, so the loop ends within 15 steps.
+__device__ __forceinline__ bool pyset_pair_lo_first(int lo, int hi, int base)
+{
+    const unsigned ia = (unsigned)(lo - base) & 7u;
+    const uint64_t h = (uint64_t)(uint32_t)(hi - base);
+    unsigned i = (unsigned)(h & 7u);
+    uint64_t perturb = h;
+    while (i == ia) {
+        perturb >>= 5;
+        i = (unsigned)((i * 5ull + 1ull + perturb) & 7u);
+    }
+    return ia < i;
+}
+
 // cells up to SMALL_CELL members are ordered by one thread with the table in local memory; larger
 // cells go to a list handled by one warp each with the table in shared memory
 constexpr int SMALL_CELL = 32;
@@ -508,11 +525,16 @@ __device__ __forceinline__ void order_small_cell(const BroadArgs& a, int g, int 
 // themselves into scatter_out, and then add 1 << 16 to the same word: the member whose add finds
 // k - 1 earlier ones (every member's write made visible by the fence before its add) orders the
 // cell, in its own thread up to SMALL_CELL members, else by the first warp of its block with the
-// tables in shared memory; it sets the count back to zero.  A cell of more than 65,535 members
-// (beyond the packed count) is written in claim order and flagged, as are cells beyond BIG_CELL,
-// which are written in ascending ids.
+// tables in shared memory; it sets the count back to zero.  (With PAIRS, of a two-member cell the
+// first member to arrive leaves its id in the count word by an atomic exchange and the second,
+// finding it there, places both.)  Cells beyond BIG_CELL members are written in ascending ids, beyond
+// 65,535 (the packed count) in claim order; both are flagged MWD_ST_CELL_CROWDED.
 constexpr int PLACE_THREADS = 128;
 constexpr int PACKED_MAX = 0xffff;
+// PAIRS: two-member cells take the exchange path below instead of the claim-and-count one -- on the
+// large row counts that launch this instance (a shorter chain: no fence); the smaller counts keep the
+// smaller kernel, whose code is fetched cold after the L2 flush of a short step
+template <bool PAIRS>
 __global__ void __launch_bounds__(PLACE_THREADS) place_kernel(BroadArgs a)
 {
     pdl_wait();
@@ -546,6 +568,19 @@ __global__ void __launch_bounds__(PLACE_THREADS) place_kernel(BroadArgs a)
                 if (a.sorted_pos) {
                     a.sorted_pos[s] = make_float4((float)pr.x, (float)pr.y, (float)pr.z, (float)pr.w);
                     a.sorted_cell[s] = g;
+                }
+            } else if (PAIRS && k == 2) {
+                // the first member leaves its id in the count word (flagged), the second finds it there,
+                // orders both and sets the word back to zero: the id travels in the atomic, no fence
+                const unsigned prev = atomicExch(reinterpret_cast<unsigned*>(cnt), 0x80000000u | (unsigned)r);
+                if (prev & 0x80000000u) {
+                    *cnt = 0;
+                    const int o = (int)(prev & 0x7fffffffu);
+                    const int lo = min(r, o), hi = max(r, o);
+                    const int base = a.info ? a.scenes[scene_of(a, lo)].row_begin : 0;
+                    const bool lo_first = pyset_pair_lo_first(lo, hi, base);
+                    place(a, s + (lo_first ? 0 : 1), lo, g);
+                    place(a, s + (lo_first ? 1 : 0), hi, g);
                 }
             } else if (k > PACKED_MAX) {
                 const int slot = atomicSub(cnt, 1) - 1;
@@ -1011,7 +1046,12 @@ int launch_broad(const BroadArgs& a_in, cudaStream_t s)
         rc = launch_scan(a.cell_count, a.total_cells, a.cell_start, a.scan_tmp, nullptr, INT64_MAX, nullptr, 0, s);
         if (rc) return rc;
     }
-    MWD_CUDA(launch_pdl(place_kernel, blocks(rows, PLACE_THREADS), PLACE_THREADS, 0, s, a));
+    // the two-member exchange path from two full waves of place blocks up (a 256-scene batch of 2M
+    // rows: broad phase 0.221 -> 0.211 ms; a 20k-row pour is 1-2 us slower with it)
+    if (rows >= 2 * (int64_t)num_sms() * (2048 / PLACE_THREADS) * PLACE_THREADS)
+        MWD_CUDA(launch_pdl(place_kernel<true>, blocks(rows, PLACE_THREADS), PLACE_THREADS, 0, s, a));
+    else
+        MWD_CUDA(launch_pdl(place_kernel<false>, blocks(rows, PLACE_THREADS), PLACE_THREADS, 0, s, a));
     // rows that have a cell are at most `rows`; threads past cell_start[total] exit
     if (a.append) {
         // split each row's walk over APPEND_PARTS threads while the rows alone leave the GPU short of

@@ -30,6 +30,30 @@ def test_linked_cell_hash_matches(seed, n, spread):
     assert pairset(got) == pairset(ref)
 
 
+def test_linked_cell_hash_many_rows_matches():
+    # 700,000 rows: enough for the place pass's large-count instance (two-member cells by an atomic
+    # exchange); 78k two-member and 121k larger cells; the oriented pairs compared as sorted int64 codes
+    import torch
+    from mwdiem_gb300 import _lib
+    rng = np.random.default_rng(21)
+    n = 700_000
+    com = rng.uniform([-100, -100, -3], [100, 100, 60], size=(n, 3))
+    keys = oracle.cell_keys(com, 2.0, 2.0, 2.0, 100, 100)
+    ref = oracle.linked_cell_hash(0, n, keys, 100, 100).astype(np.int64)
+    cap = len(ref) + 1024
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    pairs = torch.zeros((cap, 2), dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
+    k = torch.from_numpy(keys).cuda()
+    _lib.check(_lib.lib().mwd_linked_cell_hash(0, n, k.data_ptr(), 100, 100, pairs.data_ptr(), cap, cnt.data_ptr(),
+                                               st.data_ptr(), None))
+    torch.cuda.synchronize()
+    got = pairs[: int(cnt.item())].cpu().numpy().astype(np.int64)
+    assert int(st.item()) == 0 and len(got) == len(ref)
+    code = lambda p: np.sort((p[:, 0] << 32) | p[:, 1])
+    assert np.array_equal(code(got), code(ref))
+
+
 def test_crowded_cells_and_negative_keys():
     from mwdiem_gb300 import LIBRARY_Coarse_contact_detection as CCD
     rng = np.random.default_rng(3)
