@@ -535,26 +535,40 @@ __device__ void epa(const Group<LPP>& g, EpaMem& m, const float4* hA, int nA, co
         }
         g.sync();
         // horizon edges of the deleted faces, in face order then edge order (0,1),(1,2),(2,0);
-        // an edge is kept when fewer than two delpair increments land on it (.cu:482-544)
+        // an edge is kept when fewer than two delpair increments land on it (.cu:482-544), i.e. when
+        // its unordered vertex pair occurs once among the deleted faces' edges (a face's vertex indices
+        // are distinct).  When all those edges fit the group's lanes at once, one match over the lanes'
+        // vertex pairs counts them; otherwise each lane counts its edge against the deleted list.
         int nnew = 0;
         bool overflow = false;
+        const bool one_trip = 3 * ndel <= LPP;
         for (int base = 0; base < 3 * ndel; base += LPP) {
             int c = base + g.lane;
             bool keep = false;
             int e0 = 0, e1 = 0;
+            unsigned pair_code = 0x10000u + (unsigned)g.lane;  // distinct for lanes without an edge
             if (c < 3 * ndel) {
                 uint32_t t = m.del[c / 3];
                 int k = c % 3;
                 e0 = ft_v(t, k);
                 e1 = ft_v(t, k == 2 ? 0 : k + 1);
-                int cnt = 0;
-                for (int j = 0; j < ndel; ++j) {
-                    uint32_t u = m.del[j];
-                    int x = ft_v(u, 0), y = ft_v(u, 1), z = ft_v(u, 2);
-                    cnt += (e0 == y && e1 == x) + (e0 == x && e1 == y) + (e0 == z && e1 == y) +
-                           (e0 == y && e1 == z) + (e0 == x && e1 == z) + (e0 == z && e1 == x);
+                pair_code = (unsigned)(min(e0, e1) * 256 + max(e0, e1));
+                if (!one_trip) {
+                    int cnt = 0;
+                    for (int j = 0; j < ndel; ++j) {
+                        uint32_t u = m.del[j];
+                        int x = ft_v(u, 0), y = ft_v(u, 1), z = ft_v(u, 2);
+                        cnt += (e0 == y && e1 == x) + (e0 == x && e1 == y) + (e0 == z && e1 == y) +
+                               (e0 == y && e1 == z) + (e0 == x && e1 == z) + (e0 == z && e1 == x);
+                    }
+                    keep = cnt < 2;
                 }
-                keep = cnt < 2;
+            }
+            if (one_trip) {
+                // every lane of the group takes part in the match (lanes without an edge hold a code no
+                // other lane holds)
+                const unsigned same = __match_any_sync(g.mask, pair_code);
+                keep = c < 3 * ndel && __popc(same) == 1;
             }
             unsigned b = g.ballot(keep);
             if (keep) {
