@@ -47,7 +47,8 @@ enum {
     MWD_ST_HIST_OVERFLOW = 1024u   /* persistent history: more contacts than the history table holds */
 };
 
-#define MWD_EPA_FACE_CAP 128   /* live EPA faces per pair (the list is compacted as faces are deleted) */
+#define MWD_EPA_FACE_CAP 128   /* EPA faces per pair, deleted ones included as in the reference (a pair
+                                  that needs more runs again with the deleted faces removed) */
 #define MWD_EPA_COUNT_INTS 256 /* ints of mwd_work.epa_count */
 #define MWD_EPA_VERT_CAP 32    /* EPA polytope vertices per pair (4 + 25 iterations + 1) */
 #define MWD_HULL_CAP 64        /* hull vertices per side staged in shared memory */
