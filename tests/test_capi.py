@@ -71,3 +71,16 @@ def test_mirrored_row_pass_checks_its_block():
     st.xform = None
     rc = h.mwd_integrate_rows_mirror(ctypes.byref(st), scenes, None, mirror, base, off, None)
     assert rc == _lib.MWD_ERR_INVALID
+
+
+def test_cell_table_choice():
+    # which cell table mwd_broadphase uses (host logic, no device call): automatic and explicit dense
+    # give the dense table; the compressed one only where its arrays fit inside the dense ones
+    from mwdiem_gb300 import _lib
+    h = _lib.lib()
+    assert h.mwd_cell_table(2_000_000, 15_200_000, 0) == 1
+    assert h.mwd_cell_table(2_000_000, 15_200_000, 1) == 1
+    assert h.mwd_cell_table(2_000_000, 15_200_000, 2) == 2
+    assert h.mwd_cell_table(20_000, 140_005, 2) == 2
+    assert h.mwd_cell_table(20_000, 20_000 * 4 + 4095, 2) == 1   # below 4 n + 4096 cells
+    assert h.mwd_cell_table(0, 1_000_000, 2) == 1
