@@ -283,8 +283,9 @@ typedef struct {
 int mwd_inlet_step(mwd_state* st, const mwd_inlet* inlet, mwd_stream_t stream);
 
 typedef struct {
-    int32_t* cell_count;   /* (total_cells,) zero on entry, left zero on exit */
-    int32_t* cell_start;   /* (total_cells + 1,) */
+    int32_t* cell_count;   /* (total_cells,) zero on entry, left zero on exit; with cell_table = 2 the
+                              count mwd_cell_table_ints gives suffices */
+    int32_t* cell_start;   /* (total_cells + 1,), or with cell_table = 2 mwd_cell_table_ints's count */
     int32_t* cell_of;      /* (n,) global cell of each row, -1 for walls */
     int32_t* sorted;       /* (n,) rows ordered by cell, members in CPython set order */
     int32_t* pair_count;   /* (n + 1,) per-row candidate counts, then their exclusive scan */
@@ -352,6 +353,11 @@ int32_t mwd_integrate_kernels(int64_t n);
 /* The cell table mwd_broadphase uses for n rows, total_cells cells and mwd_work.cell_table = mode:
  * 1 dense, 2 occupancy-compressed.  Host utility; no reference counterpart. */
 int32_t mwd_cell_table(int64_t n, int64_t total_cells, int32_t mode);
+
+/* mwd_cell_table, and the ints mwd_work.cell_count and cell_start need for that table: total_cells
+ * and total_cells + 1 for the dense one; for the compressed one a bit per cell (three copies) and a
+ * count and a start per row, a small fraction of the dense table's size on a sparse domain. */
+int32_t mwd_cell_table_ints(int64_t n, int64_t total_cells, int32_t mode, int64_t* count_ints, int64_t* start_ints);
 
 /* One broad phase over all scenes (rows of every scene; walls excluded from the cell hash). */
 int mwd_broadphase(const mwd_state* st, const mwd_scene* scenes_dev, const mwd_scene* scenes_host,

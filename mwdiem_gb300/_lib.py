@@ -157,6 +157,7 @@ def lib():
             "mwd_scan_tmp_ints": (i64, [i64]),
             "mwd_cell_table": (i32, [i64, i64, i32]),
             "mwd_integrate_kernels": (i32, [i64]),
+            "mwd_cell_table_ints": (i32, [i64, i64, i32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
             "mwd_derive_material": (C.c_int, [C.POINTER(ContactParams), C.POINTER(Material)]),
             "mwd_contact_pairs": (C.c_int, [i64, i32, i32] + [_P] * 20 + [C.POINTER(ContactParams), _P, _P, _P]),
             "mwd_verlet_ref": (C.c_int, [i32] + [_P] * 16 + [C.POINTER(VerletParams), _P, _P]),
@@ -191,7 +192,7 @@ def lib():
         return h
 
 
-EXPORTED = ("mwd_last_error", "mwd_version", "mwd_num_sms", "mwd_scan_tmp_ints", "mwd_cell_table", "mwd_integrate_kernels",
+EXPORTED = ("mwd_last_error", "mwd_version", "mwd_num_sms", "mwd_scan_tmp_ints", "mwd_cell_table", "mwd_cell_table_ints", "mwd_integrate_kernels",
             "mwd_derive_material",
             "mwd_contact_pairs", "mwd_verlet_ref", "mwd_cell_keys", "mwd_wall_pairs", "mwd_linked_cell_hash",
             "mwd_broadphase", "mwd_narrow_force", "mwd_integrate", "mwd_step", "mwd_refresh_vertices",

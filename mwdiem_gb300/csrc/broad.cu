@@ -999,6 +999,18 @@ int broad_sparse(int64_t rows, int64_t total_cells, int64_t tile_sum_ints, int m
     return tiles <= tile_sum_ints ? 1 : 0;
 }
 
+void broad_table_ints(int64_t rows, int64_t total_cells, int sparse, int64_t* count_ints, int64_t* start_ints)
+{
+    if (sparse) {
+        const SparseLayout L = sparse_layout(rows, total_cells);
+        *count_ints = L.words_pad + L.compact_len;
+        *start_ints = 2 * L.words_pad + L.compact_len + 1;
+    } else {
+        *count_ints = total_cells > 0 ? total_cells : 1;
+        *start_ints = total_cells + 1;
+    }
+}
+
 int launch_broad(const BroadArgs& a_in, cudaStream_t s)
 {
     const int T = 128;  // row kernels: 20k rows already span every SM

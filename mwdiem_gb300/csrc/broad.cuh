@@ -52,6 +52,9 @@ int launch_broad(const BroadArgs& a, cudaStream_t s);
 // 1 when launch_broad would use the occupancy-compressed table for these sizes (mode: 0 automatic,
 // 1 dense, 2 compressed where it fits)
 int broad_sparse(int64_t rows, int64_t total_cells, int64_t tile_sum_ints, int mode);
+// ints the cell_count and cell_start arrays need for that table (the compressed one carves its arrays
+// out of their first entries)
+void broad_table_ints(int64_t rows, int64_t total_cells, int sparse, int64_t* count_ints, int64_t* start_ints);
 int launch_keys(int N, const double* com, double csx, double csy, double csz, int64_t nx, int64_t ny, int64_t* keys,
                 cudaStream_t s);
 int launch_minmax(const int64_t* keys, int lo, int hi, unsigned long long* mm, cudaStream_t s);

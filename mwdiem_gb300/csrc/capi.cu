@@ -245,6 +245,16 @@ int32_t mwd_cell_table(int64_t n, int64_t total_cells, int32_t mode)
     const int64_t m = (total_cells > n ? total_cells : n) + 1;
     return broad_sparse(n, total_cells, scan_tmp_ints(m) - scan_tile_sums_offset(m), mode) ? 2 : 1;
 }
+
+int32_t mwd_cell_table_ints(int64_t n, int64_t total_cells, int32_t mode, int64_t* count_ints, int64_t* start_ints)
+{
+    const int32_t kind = mwd_cell_table(n, total_cells, mode);
+    int64_t c = 0, st = 0;
+    broad_table_ints(n, total_cells, kind == 2 ? 1 : 0, &c, &st);
+    if (count_ints) *count_ints = c;
+    if (start_ints) *start_ints = st;
+    return kind;
+}
 int64_t mwd_det_scratch_bytes(int32_t n, int64_t epa_cap)
 {
     return n < 0 || epa_cap < 0 ? -1 : (int64_t)det_scratch_bytes(n, epa_cap);

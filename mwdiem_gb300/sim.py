@@ -67,8 +67,9 @@ class Simulator:
         self.deterministic = bool(deterministic)
         self.persistent_history = bool(persistent_history)
         # the broad phase's cell table: "dense" (a count and a start per cell), "compressed" (a bit per
-        # cell, counts and starts per occupied cell; where it fits), or "auto" (dense, the faster of
-        # the two on every workload measured): the same pairs either way
+        # cell, counts and starts per occupied cell, where it fits: on a sparse domain a small fraction
+        # of the dense table's memory), or "auto" (dense, the faster of the two on every workload
+        # measured): the same pairs either way
         tables = {"auto": CELL_TABLE_AUTO, "dense": CELL_TABLE_DENSE, "compressed": CELL_TABLE_COMPRESSED}
         if cell_table not in tables:
             raise ValueError(f"cell_table must be one of {sorted(tables)}")
@@ -310,8 +311,11 @@ class Simulator:
         cap = int(pair_cap) if pair_cap else max(4096, (16 if self.cull_pairs else 40) * n_part)
         i32 = dict(dtype=torch.int32, device=self.device)
         w = {}
-        w["cell_count"] = torch.zeros(max(self.total_cells, 1), **i32)
-        w["cell_start"] = torch.zeros(self.total_cells + 1, **i32)
+        # the cell table's arrays: a count and a start per cell, or the compressed table's smaller ones
+        cnt_ints, start_ints = C.c_int64(), C.c_int64()
+        lib().mwd_cell_table_ints(n, self.total_cells, self.cell_table, C.byref(cnt_ints), C.byref(start_ints))
+        w["cell_count"] = torch.zeros(max(int(cnt_ints.value), 1), **i32)
+        w["cell_start"] = torch.zeros(int(start_ints.value), **i32)
         w["cell_of"] = torch.zeros(n, **i32)
         w["sorted"] = torch.zeros(n, **i32)
         w["pair_count"] = torch.zeros(n + 1, **i32)

@@ -202,6 +202,25 @@ def test_compressed_cell_table_lists_the_dense_tables_pairs():
     b.check_status()
 
 
+def test_compressed_cell_table_on_a_sparse_domain():
+    # 5,000 hulls in a 1,550-wide box: 5.4M cells for 5,000 rows.  The compressed table's arrays take
+    # a small fraction of the dense table's memory and list the reference's oriented candidates
+    from mwdiem_gb300.sim import Simulator
+    sp = scene.pour_scene(n=5000, seed=3, box=1500.0)
+    sim = Simulator(sp, cull_pairs=False, cell_table="compressed")
+    assert sim.cell_table_in_use == "compressed" and sim.total_cells > 5_000_000
+    assert sim.w["cell_count"].numel() + sim.w["cell_start"].numel() < 0.15 * (2 * sim.total_cells + 1)
+    for _ in range(2):
+        pairs = device_pairs(sim, cull=False)
+        ref = stepper.RefStepper(sp)
+        ref.st["com"][:] = sim.t["pos"][:, :3].cpu().numpy()
+        want = ref.candidate_pairs()
+        assert len(pairs) == len(want) > 1000 and oriented(pairs) == oriented(want)
+        sim.step(5)
+        torch.cuda.synchronize()
+    sim.check_status()
+
+
 def test_narrow_4m_pairs_sample_matches_oracle():
     # the narrow-phase benchmark's own pairs (bench.py: 4M pairs, seed 1) and its lane setting
     from mwdiem_gb300.pairbench import PairScene
