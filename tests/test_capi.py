@@ -84,3 +84,19 @@ def test_cell_table_choice():
     assert h.mwd_cell_table(20_000, 140_005, 2) == 2
     assert h.mwd_cell_table(20_000, 20_000 * 4 + 4095, 2) == 1   # below 4 n + 4096 cells
     assert h.mwd_cell_table(0, 1_000_000, 2) == 1
+
+
+def test_cell_table_sizes():
+    # the ints the cell_count / cell_start arrays need for the chosen table (host logic)
+    import ctypes
+    from mwdiem_gb300 import _lib
+    h = _lib.lib()
+    c, s = ctypes.c_int64(), ctypes.c_int64()
+    assert h.mwd_cell_table_ints(20_000, 140_005, 0, ctypes.byref(c), ctypes.byref(s)) == 1
+    assert (c.value, s.value) == (140_005, 140_006)
+    assert h.mwd_cell_table_ints(5_005, 5_400_000, 2, ctypes.byref(c), ctypes.byref(s)) == 2
+    words = (5_400_000 + 31) // 32
+    pad = (words + 1 + 3) // 4 * 4
+    rows = (5_005 + 1 + 3) // 4 * 4
+    assert (c.value, s.value) == (pad + rows, 2 * pad + rows + 1)
+    assert c.value + s.value < 0.15 * (2 * 5_400_000 + 1)
