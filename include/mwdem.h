@@ -198,7 +198,10 @@ int mwd_wall_pairs(int32_t n_wall, int32_t n_lo, int32_t n_hi, const double* com
  * same-cell pairs oriented in CPython set iteration order, cross-cell pairs for the offsets
  * +1, +nx, +nx*ny, +nx*ny+1, +nx*ny+1+nx, +nx*ny+nx, +nx+1 with A from the lower-offset cell.
  * The emitted SET of oriented pairs equals the reference list; the list order is by cell.
- * keys: (n_hi,) i64 (rows below n_lo ignored).  pairs (cap,2) i32; n_out device int64 (total). */
+ * keys: (n_hi,) i64 (rows below n_lo ignored).  pairs (cap,2) i32; n_out device int64 (total).
+ * A key range (max - min + 1) up to 2^28 cells takes a dense cell table; wider ranges, up to 2^31
+ * cells with at most about a quarter as many ids, the occupancy-compressed one (MWD_ERR_UNSUPPORTED
+ * beyond). */
 int mwd_linked_cell_hash(int32_t n_lo, int32_t n_hi, const int64_t* keys, int64_t nx, int64_t ny,
                          int32_t* pairs, int64_t cap, int64_t* n_out, uint32_t* status,
                          mwd_stream_t stream);

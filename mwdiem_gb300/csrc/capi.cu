@@ -429,20 +429,28 @@ int mwd_linked_cell_hash(int32_t n_lo, int32_t n_hi, const int64_t* keys, int64_
     const int64_t kmin = (int64_t)(mm[0] ^ 0x8000000000000000ull);
     const int64_t kmax = (int64_t)(mm[1] ^ 0x8000000000000000ull);
     const int64_t R = kmax - kmin + 1;
-    if (R <= 0 || R > (int64_t)1 << 28) {
-        set_error("cell key range %lld is too wide for a dense cell table", (long long)R);
+    const int64_t rows = n_hi - n_lo;
+    const int64_t m = (R > rows ? R : rows) + 1;
+    // a dense cell table up to 2^28 cells; beyond, the compressed one (a bit per cell, a count and a
+    // start per row), which a sparse key range of up to 2^31 cells fits
+    int sparse = 0;
+    if (R > (int64_t)1 << 28)
+        sparse = R <= INT32_MAX - 64 ? broad_sparse(rows, R, scan_tmp_ints(m) - scan_tile_sums_offset(m), 2) : 0;
+    if (R <= 0 || (R > (int64_t)1 << 28 && !sparse)) {
+        set_error("cell key range %lld is too wide for the cell tables", (long long)R);
         return MWD_ERR_UNSUPPORTED;
     }
-    const int64_t rows = n_hi - n_lo;
+    int64_t count_ints = 0, start_ints = 0;
+    broad_table_ints(rows, R, sparse, &count_ints, &start_ints);
     Carver c;
     size_t o_scene = c.take<mwd_scene>(1);
-    size_t o_count = c.take<int32_t>(R);
-    size_t o_start = c.take<int32_t>(R + 1);
+    size_t o_count = c.take<int32_t>(count_ints);
+    size_t o_start = c.take<int32_t>(start_ints);
     size_t o_cellof = c.take<int32_t>(n_hi);
     size_t o_scat = c.take<int32_t>(n_hi);
     size_t o_sorted = c.take<int32_t>(n_hi);
     size_t o_pc = c.take<int32_t>(rows + 1);
-    size_t o_tmp = c.take<int32_t>(scan_tmp_ints(R > rows ? R + 1 : rows + 1));
+    size_t o_tmp = c.take<int32_t>(scan_tmp_ints(m));
     rc = scratch(c.off, &base);
     if (rc) return rc;
     char* b = (char*)base;
@@ -453,7 +461,12 @@ int mwd_linked_cell_hash(int32_t n_lo, int32_t n_hi, const int64_t* keys, int64_
     sc.n_keys = R;
     sc.cell_base = 0;
     MWD_CUDA(cudaMemcpyAsync(b + o_scene, &sc, sizeof(sc), cudaMemcpyHostToDevice, s));
-    MWD_CUDA(cudaMemsetAsync(b + o_count, 0, R * sizeof(int32_t), s));
+    MWD_CUDA(cudaMemsetAsync(b + o_count, 0, count_ints * sizeof(int32_t), s));
+    int32_t* tile_sums = nullptr;
+    if (sparse) {  // the compressed table's per-tile counts, zero on entry
+        tile_sums = reinterpret_cast<int32_t*>(b + o_tmp) + scan_tile_sums_offset(m);
+        MWD_CUDA(cudaMemsetAsync(tile_sums, 0, (scan_tmp_ints(m) - scan_tile_sums_offset(m)) * sizeof(int32_t), s));
+    }
     BroadArgs a = {};
     a.row_lo = n_lo;
     a.row_hi = n_hi;
@@ -472,6 +485,8 @@ int mwd_linked_cell_hash(int32_t n_lo, int32_t n_hi, const int64_t* keys, int64_
     a.status = status;
     a.total_cells = R;
     a.pair_cap = cap;
+    a.tile_sums = tile_sums;
+    a.sparse = sparse;
     rc = launch_broad(a, s);
     if (rc) return rc;
     // the host copy of the scene must outlive the async copy

@@ -54,6 +54,20 @@ def test_linked_cell_hash_many_rows_matches():
     assert np.array_equal(code(got), code(ref))
 
 
+def test_linked_cell_hash_wide_key_range_matches():
+    # a key range of ~7e8 cells (beyond the dense table's 2^28) for 60,000 ids: the compressed table
+    from mwdiem_gb300 import LIBRARY_Coarse_contact_detection as CCD
+    rng = np.random.default_rng(23)
+    n = 60_000
+    com = rng.uniform([-20000, -20000, -3], [20000, 20000, 3], size=(n, 3))
+    com[: n // 2, :2] = rng.uniform(-150, 150, size=(n // 2, 2))  # a dense patch, so pairs exist
+    keys = oracle.cell_keys(com, 2.0, 2.0, 2.0, 20000, 20000)
+    assert keys.max() - keys.min() + 1 > (1 << 28)
+    ref = oracle.linked_cell_hash(0, n, keys, 20000, 20000)
+    got = CCD.Linked_cell_hash(None, 20000, 20000, 0, n, [], keys)
+    assert len(ref) > 1000 and len(got) == len(ref) and pairset(got) == pairset(ref)
+
+
 def test_crowded_cells_and_negative_keys():
     from mwdiem_gb300 import LIBRARY_Coarse_contact_detection as CCD
     rng = np.random.default_rng(3)
