@@ -311,10 +311,11 @@ typedef struct {
     int32_t cull_pairs;    /* 1: the broad phase lists only pairs whose bounding spheres (pos.w) overlap
                               within a rounding margin -- the others are exactly the candidates the
                               reference's first GJK test rejects; 0: the reference's full candidate list */
-    int32_t cell_table;    /* layout of cell_count / cell_start: 0 automatic (dense), 1 dense (a count
-                              and a start per cell), 2 occupancy-compressed where it fits (a bit per
-                              cell, counts and starts per occupied cell, carved out of the same two
-                              arrays; needs total_cells >= 4 n + 4096).  The same pairs either way. */
+    int32_t cell_table;    /* layout of cell_count / cell_start: 0 automatic (dense up to 2^27 cells,
+                              compressed beyond where it fits), 1 dense (a count and a start per cell),
+                              2 occupancy-compressed where it fits (a bit per cell, counts and starts
+                              per occupied cell, carved out of the same two arrays; needs total_cells >=
+                              4 n + 4096).  The same pairs either way. */
     int64_t total_cells;
     int64_t pair_cap;
     int32_t* face_ids;     /* optional (pair_cap, 6): support-vertex indices (into each row's vertex table)

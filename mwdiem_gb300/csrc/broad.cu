@@ -985,11 +985,13 @@ SparseLayout sparse_layout(int64_t rows, int64_t total_cells)
 
 int broad_sparse(int64_t rows, int64_t total_cells, int64_t tile_sum_ints, int mode)
 {
-    // automatic: the dense table.  On 256 batched scenes (2.0M rows, 15.2M cells) the compressed table
+    // automatic: the dense table up to 2^27 cells (1 GB of count and start arrays), the compressed one
+    // beyond where it fits.  On 256 batched scenes (2.0M rows, 15.2M cells) the compressed table
     // measured slower (broad phase 0.263 vs 0.229 ms): its lower atomic and scan traffic does not pay for
     // the extra level of dependent loads (bit word and rank before each range) in the place and append
-    // passes and its two more launches.
-    if (mode != 2 || tile_sum_ints <= 0 || rows <= 0) return 0;
+    // passes and its two more launches; on a sparse domain it takes a fraction of the memory.
+    if (mode == 1 || tile_sum_ints <= 0 || rows <= 0) return 0;
+    if (mode == 0 && total_cells <= ((int64_t)1 << 27)) return 0;
     if (total_cells < 4 * rows + 4096 || total_cells > INT32_MAX - 64) return 0;
     const SparseLayout L = sparse_layout(rows, total_cells);
     // the carved arrays fit in cell_count (total_cells ints) and cell_start (total_cells + 1)

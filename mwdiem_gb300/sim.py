@@ -69,7 +69,7 @@ class Simulator:
         # the broad phase's cell table: "dense" (a count and a start per cell), "compressed" (a bit per
         # cell, counts and starts per occupied cell, where it fits: on a sparse domain a small fraction
         # of the dense table's memory), or "auto" (dense, the faster of the two on every workload
-        # measured): the same pairs either way
+        # measured, up to 2^27 cells; compressed beyond, where it fits): the same pairs either way
         tables = {"auto": CELL_TABLE_AUTO, "dense": CELL_TABLE_DENSE, "compressed": CELL_TABLE_COMPRESSED}
         if cell_table not in tables:
             raise ValueError(f"cell_table must be one of {sorted(tables)}")
@@ -299,6 +299,8 @@ class Simulator:
             sc.law.law = CONTACT_LAWS[sp.law]
             check(lib().mwd_derive_material(C.byref(sc.law), sc.mat))
         self.scenes_host = arr
+        if base > (1 << 31) - 64:
+            raise ValueError(f"{base} cells: the cell tables index cells with 32-bit integers (at most 2^31 - 64)")
         self.total_cells = base
         raw = bytes(C.string_at(C.addressof(arr), C.sizeof(arr)))
         self.scenes_dev = torch.frombuffer(bytearray(raw), dtype=torch.uint8).to(self.device)

@@ -187,7 +187,7 @@ def test_compressed_cell_table_lists_the_dense_tables_pairs():
     a = Simulator(spec, cull_pairs=True, deterministic=True, cell_table="dense")
     b = Simulator(spec, cull_pairs=True, deterministic=True, cell_table="compressed")
     assert a.cell_table_in_use == "dense" and b.cell_table_in_use == "compressed"
-    assert Simulator(spec).cell_table_in_use == "dense"   # automatic: the dense table
+    assert Simulator(spec).cell_table_in_use == "dense"   # automatic: the dense table (140k cells)
     for _ in range(3):
         for cull in (False, True):
             pa, pb = device_pairs(a, cull), device_pairs(b, cull)

@@ -79,6 +79,7 @@ def test_cell_table_choice():
     from mwdiem_gb300 import _lib
     h = _lib.lib()
     assert h.mwd_cell_table(2_000_000, 15_200_000, 0) == 1
+    assert h.mwd_cell_table(2_000_000, 300_000_000, 0) == 2   # automatic: beyond 2^27 cells
     assert h.mwd_cell_table(2_000_000, 15_200_000, 1) == 1
     assert h.mwd_cell_table(2_000_000, 15_200_000, 2) == 2
     assert h.mwd_cell_table(20_000, 140_005, 2) == 2
