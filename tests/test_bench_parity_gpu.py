@@ -202,13 +202,15 @@ def test_compressed_cell_table_lists_the_dense_tables_pairs():
     b.check_status()
 
 
-def test_compressed_cell_table_on_a_sparse_domain():
-    # 5,000 hulls in a 1,550-wide box: 5.4M cells for 5,000 rows.  The compressed table's arrays take
-    # a small fraction of the dense table's memory and list the reference's oriented candidates
+@pytest.mark.parametrize("box,table,cells", [(1500.0, "compressed", 5_000_000), (8000.0, "auto", 1 << 27)])
+def test_compressed_cell_table_on_a_sparse_domain(box, table, cells):
+    # 5,000 hulls in a 1,550-wide box (5.4M cells; the compressed table on request) and in an
+    # 8,050-wide one (beyond 2^27 cells: the automatic choice).  The compressed table's arrays take a
+    # small fraction of the dense table's memory and list the reference's oriented candidates
     from mwdiem_gb300.sim import Simulator
-    sp = scene.pour_scene(n=5000, seed=3, box=1500.0)
-    sim = Simulator(sp, cull_pairs=False, cell_table="compressed")
-    assert sim.cell_table_in_use == "compressed" and sim.total_cells > 5_000_000
+    sp = scene.pour_scene(n=5000, seed=3, box=box)
+    sim = Simulator(sp, cull_pairs=False, cell_table=table)
+    assert sim.cell_table_in_use == "compressed" and sim.total_cells > cells
     assert sim.w["cell_count"].numel() + sim.w["cell_start"].numel() < 0.15 * (2 * sim.total_cells + 1)
     for _ in range(2):
         pairs = device_pairs(sim, cull=False)
